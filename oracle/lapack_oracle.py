@@ -1,0 +1,181 @@
+"""TEST INFRASTRUCTURE — parity oracle for batched eigenvalue-only ZGEEV.
+
+Only ``tests/``, ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline
+leg may use this module; the product never does.
+
+Oracle = LAPACK zgeev with JOBVL = JOBVR = 'N' in FP64, the routine the
+reference compares against (stream_test_with_MKL/get_eig_MKL.c:33-46 calls
+MKL's LAPACKE_zgeev(LAPACK_COL_MAJOR, 'N', 'N', ...)). MKL is an un-vendored,
+unpinned dependency of the reference and is absent here; the same published
+LAPACK routine is taken from the OpenBLAS 0.3.34 LAPACK bundled with scipy
+1.18.1 (symbols ``scipy_LAPACKE_zgeev`` / ``scipy_LAPACKE_zgeevx``), driven
+from the small C harness ``oracle/cpu_zgeev.c``. That harness also serves as
+the timed CPU baseline (one zgeev per matrix, threads over the batch, as
+get_eig_MKL.c:26-51 does with OpenMP).
+
+The parity metric replaces the reference's sort-based relative error
+(stream_test_with_MKL/main.cu:16-181): eigenvalues are matched per matrix by
+an optimal assignment (Hungarian method) and the error is
+max |lambda - lambda_LAPACK| / ||A||_F, checked against 1e-11 on matrices whose
+eigenvalue condition numbers (1/RCONDE from zgeevx, no balancing) are <= 1e3.
+"""
+from __future__ import annotations
+
+import ctypes
+import glob
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD_DIR = os.path.join(HERE, "_build")
+LIB_PATH = os.path.join(BUILD_DIR, "libcpu_zgeev.so")
+SRC = os.path.join(HERE, "cpu_zgeev.c")
+
+TOL_REL_FRO = 1e-11
+COND_MAX = 1e3
+
+_lib = None
+
+
+def find_lapack() -> str:
+    """Path of the LAPACK shared library bundled with scipy (LP64 OpenBLAS)."""
+    import scipy
+
+    root = os.path.dirname(os.path.dirname(scipy.__file__))
+    cands = sorted(glob.glob(os.path.join(root, "scipy.libs", "libscipy_openblas*.so*")))
+    if not cands:
+        raise RuntimeError("scipy's bundled OpenBLAS (scipy.libs/libscipy_openblas*.so) not found")
+    return cands[0]
+
+
+def build(force: bool = False) -> str:
+    """Compiles the C harness with gcc (plain C, no vendored sources)."""
+    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= os.path.getmtime(SRC):
+        return LIB_PATH
+    os.makedirs(BUILD_DIR, exist_ok=True)
+    tmp = LIB_PATH + ".tmp"
+    cmd = ["gcc", "-O2", "-std=c11", "-shared", "-fPIC", "-o", tmp, SRC, "-ldl", "-lpthread"]
+    subprocess.run(cmd, check=True, capture_output=True)
+    os.replace(tmp, LIB_PATH)
+    return LIB_PATH
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        build()
+        lib = ctypes.CDLL(LIB_PATH)
+        lib.cpu_zgeev_open.argtypes = [ctypes.c_char_p]
+        lib.cpu_zgeev_batched.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+        lib.cpu_zgeevx_batched.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                           ctypes.POINTER(ctypes.c_double)]
+        st = lib.cpu_zgeev_open(find_lapack().encode())
+        if st != 0:
+            raise RuntimeError(f"cannot open LAPACK ({st})")
+        _lib = lib
+    return _lib
+
+
+def default_threads() -> int:
+    return max(1, len(os.sched_getaffinity(0)))
+
+
+def _as_batch(A: np.ndarray) -> np.ndarray:
+    A = np.ascontiguousarray(A, dtype=np.complex128)
+    if A.ndim == 2:
+        A = A[None]
+    return A
+
+
+def zgeev(A: np.ndarray, threads: int | None = None):
+    """LAPACK zgeev('N','N') per matrix.
+
+    ``A[k]`` is read as the column-major buffer of matrix k, i.e. the
+    eigenvalues returned are those of ``A[k].T`` — identical to those of
+    ``A[k]``. Returns ``(w[batch, n], info[batch], seconds)``.
+    """
+    lib = _load()
+    A = _as_batch(A)
+    b, n, _ = A.shape
+    w = np.empty((b, n), np.complex128)
+    info = np.empty(b, np.int32)
+    sec = ctypes.c_double()
+    lib.cpu_zgeev_batched(n, b, A.ctypes.data, w.ctypes.data, info.ctypes.data, threads or default_threads(),
+                          ctypes.byref(sec))
+    return w, info, sec.value
+
+
+def zgeevx_rconde(A: np.ndarray, threads: int | None = None):
+    """zgeevx(BALANC='N', SENSE='E'): ``(w, rconde, info)`` per matrix."""
+    lib = _load()
+    A = _as_batch(A)
+    b, n, _ = A.shape
+    w = np.empty((b, n), np.complex128)
+    rc = np.empty((b, n), np.float64)
+    info = np.empty(b, np.int32)
+    sec = ctypes.c_double()
+    lib.cpu_zgeevx_batched(n, b, A.ctypes.data, w.ctypes.data, rc.ctypes.data, info.ctypes.data,
+                           threads or default_threads(), ctypes.byref(sec))
+    return w, rc, info
+
+
+def matched_abs_errors(w_test: np.ndarray, w_ref: np.ndarray) -> np.ndarray:
+    """Per-eigenvalue |error| after optimal per-matrix matching; shape [batch, n], in w_ref's order."""
+    from scipy.optimize import linear_sum_assignment
+
+    w_test = np.atleast_2d(w_test)
+    w_ref = np.atleast_2d(w_ref)
+    out = np.empty(w_ref.shape, np.float64)
+    for k in range(w_ref.shape[0]):
+        a, b = w_ref[k], w_test[k]
+        d = np.abs(a[:, None] - b[None, :])
+        if not np.all(np.isfinite(d)):
+            out[k] = np.inf
+            continue
+        # Fast path: nearest neighbours already form a permutation.
+        nn = np.argmin(d, axis=1)
+        if len(np.unique(nn)) == len(nn):
+            out[k] = d[np.arange(len(a)), nn]
+            # nearest-neighbour assignment is optimal for the max metric only if no
+            # other permutation lowers the maximum; verify with the Hungarian method
+            # when the errors are not tiny compared to the gaps.
+            gaps = np.sort(d, axis=1)
+            if gaps.shape[1] < 2 or np.all(out[k] * 4 < gaps[:, 1]):
+                continue
+        r, c = linear_sum_assignment(d)
+        out[k][r] = d[r, c]
+    return out
+
+
+def parity_report(A: np.ndarray, w_test: np.ndarray, flag_test: np.ndarray, threads: int | None = None,
+                  with_cond: bool = True) -> dict:
+    """Compares eigenvalues/flags against LAPACK zgeev on the same inputs."""
+    A = _as_batch(A)
+    w_ref, info, _ = zgeev(A, threads)
+    fro = np.sqrt(np.sum(np.abs(A) ** 2, axis=(1, 2)))
+    fro = np.where(fro == 0, 1.0, fro)
+    ok = (info == 0) & (np.asarray(flag_test) == 0)
+    err = np.full(w_ref.shape, np.nan)
+    if ok.any():
+        err[ok] = matched_abs_errors(np.asarray(w_test)[ok], w_ref[ok])
+    rel = np.nanmax(err, axis=1) / fro
+    rep = {
+        "batch": int(A.shape[0]),
+        "flag_mismatch": int(np.sum((info != 0) != (np.asarray(flag_test) != 0))),
+        "lapack_fail": int(np.sum(info != 0)),
+        "max_rel_err": float(np.nanmax(rel)) if ok.any() else float("nan"),
+        "p99_rel_err": float(np.nanpercentile(rel[ok], 99)) if ok.any() else float("nan"),
+    }
+    if with_cond:
+        _, rc, _ = zgeevx_rconde(A, threads)
+        cond = 1.0 / np.maximum(rc, 1e-300)
+        well = ok & (np.max(cond, axis=1) <= COND_MAX)
+        rep["well_conditioned"] = int(well.sum())
+        rep["max_rel_err_well"] = float(np.nanmax(rel[well])) if well.any() else float("nan")
+        rep["p99_rel_err_well"] = float(np.nanpercentile(rel[well], 99)) if well.any() else float("nan")
+    rep["rel_err"] = rel
+    return rep

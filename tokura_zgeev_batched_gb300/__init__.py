@@ -1,0 +1,18 @@
+"""GB300-native batched eigenvalue-only ZGEEV (drop-in for tokura_zgeev_batched).
+
+The product is the C-ABI library built from ``csrc/`` (see ``include/
+tokura_blas.h``); :mod:`.api` mirrors the reference's C API from Python and
+adds torch-tensor wrappers.
+"""
+from .api import (  # noqa: F401
+    MAX_MATRIX_SIZE,
+    Handle,
+    default_handle,
+    exported_symbols,
+    lib,
+    tokura_get_zgeeveigenvaluesgetworspacesize,
+    tokura_zgeev_batched_gpu,
+    tokuraCreate,
+    tokuraDestroy,
+    zgeev_batched,
+)

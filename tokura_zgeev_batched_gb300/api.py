@@ -1,0 +1,166 @@
+"""Host-side mirror of the reference's C API, over the in-tree C-ABI library.
+
+The functions below keep the reference's names, argument order, argument
+meaning and integer return codes (tokura_zgeev_batched_library/include/
+tokura_blas.h:129-151, README.md:26-74); pointers are passed as integers
+(device addresses) and streams as ``cudaStream_t`` integers, exactly what a
+ctypes binding of the reference would pass. On top of that,
+:func:`zgeev_batched` is a torch-tensor convenience wrapper.
+
+The library must be built (``tokura_zgeev_batched_gb300.build.build()``);
+loading fails loudly otherwise — there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+from . import build as _build
+
+_LIB = None
+
+MAX_MATRIX_SIZE = 64
+
+# Exported C symbols declared in include/tokura_blas.h, with ctypes signatures.
+_SIGNATURES = {
+    "tokuraCreate": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p)]),
+    "tokuraDestroy": (ctypes.c_int, [ctypes.c_void_p]),
+    "tokura_get_zgeeveigenvaluesgetworspacesize": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int]),
+    "tokura_zgeev_batched_gpu": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+         ctypes.c_void_p, ctypes.c_void_p],
+    ),
+}
+
+
+def exported_symbols() -> list[str]:
+    return list(_SIGNATURES)
+
+
+def lib(autobuild: bool = True) -> ctypes.CDLL:
+    """Loads (building first if allowed and needed) the C-ABI library."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.LIB_PATH
+    if autobuild and _build.needs_build():
+        _build.build()
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: build it with tokura_zgeev_batched_gb300.build.build()")
+    handle = ctypes.CDLL(path)
+    for name, (res, args) in _SIGNATURES.items():
+        fn = getattr(handle, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = handle
+    return handle
+
+
+class Handle:
+    """Owns a ``tokurablas_t*`` (tokuraCreate/tokuraDestroy)."""
+
+    def __init__(self):
+        ptr = ctypes.c_void_p()
+        status = lib().tokuraCreate(ctypes.byref(ptr))
+        if status != 0:
+            raise RuntimeError(f"tokuraCreate failed with status {status}")
+        self.ptr = ptr
+
+    @property
+    def value(self) -> int:
+        return self.ptr.value
+
+    def close(self):
+        if self.ptr is not None and self.ptr.value:
+            lib().tokuraDestroy(self.ptr)
+        self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def tokuraCreate() -> tuple[int, Handle | None]:
+    try:
+        return 0, Handle()
+    except RuntimeError:
+        return 1, None
+
+
+def tokuraDestroy(handle: Handle | None) -> int:
+    if handle is not None:
+        handle.close()
+    return 0
+
+
+def tokura_get_zgeeveigenvaluesgetworspacesize(n: int, batch_count: int) -> int:
+    return int(lib().tokura_get_zgeeveigenvaluesgetworspacesize(int(n), int(batch_count)))
+
+
+def _ptr(h) -> int | None:
+    if h is None:
+        return None
+    if isinstance(h, Handle):
+        return h.value
+    return int(h)
+
+
+def tokura_zgeev_batched_gpu(handle, n: int, batch_count: int, A: int, eigenvalues: int, work: int, flag: int,
+                             cudastream: int = 0) -> int:
+    """Raw entry point: device addresses as integers, returns the C status."""
+    return int(lib().tokura_zgeev_batched_gpu(_ptr(handle), int(n), int(batch_count), A, eigenvalues, work, flag,
+                                              cudastream))
+
+
+_DEFAULT_HANDLE = None
+
+
+def default_handle() -> Handle:
+    global _DEFAULT_HANDLE
+    if _DEFAULT_HANDLE is None:
+        _DEFAULT_HANDLE = Handle()
+    return _DEFAULT_HANDLE
+
+
+def zgeev_batched(A, handle: Handle | None = None, work=None, stream=None):
+    """Eigenvalues of a batch of square complex128 CUDA matrices ``A[..., n, n]``.
+
+    Returns ``(eigenvalues[..., n], flag[...])`` (flag int8: 0 converged,
+    1 iteration cap hit, 2 non-finite input). A is not modified. Runs on the
+    current torch stream unless ``stream`` (a torch.cuda.Stream) is given.
+    """
+    import torch
+
+    if not A.is_cuda or A.dtype != torch.complex128:
+        raise TypeError("A must be a complex128 CUDA tensor")
+    n = A.shape[-1]
+    if A.shape[-2] != n:
+        raise ValueError("matrices must be square")
+    batch_shape = A.shape[:-2]
+    Ab = A.reshape(-1, n, n)
+    # eig(M^T) = eig(M): the row-major buffer of M is the column-major buffer of M^T.
+    Ab = Ab.contiguous()
+    batch = Ab.shape[0]
+    eig = torch.empty(batch, n, dtype=torch.complex128, device=A.device)
+    flag = torch.empty(batch, dtype=torch.int8, device=A.device)
+    if batch == 0:
+        return eig.reshape(*batch_shape, n), flag.reshape(batch_shape)
+    need = tokura_get_zgeeveigenvaluesgetworspacesize(n, batch)
+    if work is None or work.numel() * work.element_size() < need:
+        work = torch.empty(need, dtype=torch.uint8, device=A.device)
+    s = stream if stream is not None else torch.cuda.current_stream(A.device)
+    h = handle if handle is not None else default_handle()
+    status = tokura_zgeev_batched_gpu(h, n, batch, Ab.data_ptr(), eig.data_ptr(), work.data_ptr(), flag.data_ptr(),
+                                      s.cuda_stream)
+    if status != 0:
+        raise RuntimeError(f"tokura_zgeev_batched_gpu returned {status}")
+    return eig.reshape(*batch_shape, n), flag.reshape(batch_shape)

@@ -1,0 +1,60 @@
+// C-ABI layer: handle lifecycle, argument validation with the reference's
+// return codes, workspace query and dispatch to the sm_103a kernels.
+//
+// Reference interface replaced: tokura_zgeev_batched_library/src/
+// tokura_zgeev_batched.cu:64-285 (tokuraCreate, tokuraDestroy,
+// tokura_get_zgeeveigenvaluesgetworspacesize, tokura_zgeev_batched_gpu).
+// Unlike the reference, the handle is not written by calls (the reference
+// stores every call's arguments in it, tokura_zgeev_batched.cu:224-235), and
+// the NULL-handle check happens before any dereference.
+#include <new>
+
+#include "../../include/tokura_blas.h"
+#include "tokura_handle.h"
+#include "zgeev_internal.h"
+
+using tzg::PlainConfig;
+
+extern "C" int tokuraCreate(tokurablas_t** handle) {
+  if (handle == nullptr) return -1;
+  tokurablas_t* h = new (std::nothrow) tokurablas_t();
+  if (h == nullptr) return -1;
+  if (cudaGetDevice(&h->device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&h->sm_count, cudaDevAttrMultiProcessorCount, h->device) != cudaSuccess) {
+    delete h;
+    return 1;
+  }
+  tzg::init_default_tuning(h);
+  *handle = h;
+  return 0;
+}
+
+extern "C" int tokuraDestroy(tokurablas_t* handle) {
+  delete handle;
+  return 0;
+}
+
+extern "C" size_t tokura_get_zgeeveigenvaluesgetworspacesize(int n, int batch_count) {
+  if (!(0 < n && n <= TOKURA_ZGEEV_BATCHED_MAX_MATRIX_SIZE)) return (size_t)-1;
+  if (!(0 < batch_count)) return (size_t)-2;
+  const size_t nn = (size_t)n * (size_t)n;
+  return sizeof(cuDoubleComplex) * nn * (size_t)batch_count + sizeof(cuDoubleComplex) * (size_t)n * (size_t)batch_count;
+}
+
+extern "C" int tokura_zgeev_batched_gpu(tokurablas_t* handle, int n, int batch_count, cuDoubleComplex* A,
+                                        cuDoubleComplex* eigenvalues, cuDoubleComplex* work, char* flag,
+                                        cudaStream_t cudastream) {
+  if (handle == nullptr) return -1;
+  if (!(n > 0 && n <= TOKURA_ZGEEV_BATCHED_MAX_MATRIX_SIZE)) return -2;
+  if (A == nullptr) return -3;
+  if (eigenvalues == nullptr) return -4;
+  if (work == nullptr) return -5;
+  if (!(batch_count > 0)) return -6;
+  if (flag == nullptr) return -7;
+  const PlainConfig cfg = tzg::plain_config_for(handle, n, batch_count);
+  const int itmax = handle->itmax_override > 0 ? handle->itmax_override : tzg::default_itmax(n);
+  const cudaError_t err = tzg::launch_plain(cfg, n, batch_count, reinterpret_cast<const double2*>(A),
+                                            reinterpret_cast<double2*>(eigenvalues),
+                                            reinterpret_cast<double2*>(work), flag, itmax, cudastream);
+  return err == cudaSuccess ? 0 : 1;
+}

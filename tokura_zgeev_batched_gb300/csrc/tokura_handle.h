@@ -1,0 +1,39 @@
+// Contents of the opaque tokurablas_t handle and the launch-shape policy.
+#pragma once
+
+#include "zgeev_internal.h"
+
+struct tokurablas_t {
+  int device = 0;
+  int sm_count = 0;
+  int itmax_override = 0;  // >0 replaces the per-eigenvalue sweep cap 30*max(10,n)
+  // Tuned plain-kernel shape per n (index 1..64); lanes == 0 means "heuristic".
+  tzg::PlainConfig plain[65] = {};
+};
+
+namespace tzg {
+
+inline void init_default_tuning(tokurablas_t* h) {
+  for (int n = 0; n <= 64; ++n) h->plain[n] = PlainConfig{0, 128};
+}
+
+// Lanes per matrix: enough lane groups to give every SM sub-partition at
+// least two warps (FP64 saturates at one warp per sub-partition; the second
+// hides memory latency); otherwise spread each matrix over more lanes.
+inline PlainConfig plain_config_for(const tokurablas_t* h, int n, int batch) {
+  PlainConfig c = h->plain[n];
+  if (c.lanes == 0) {
+    const long long want_lanes = (long long)h->sm_count * 4 * 2 * 32;
+    if ((long long)batch >= want_lanes)
+      c.lanes = 1;
+    else if ((long long)batch * 2 >= want_lanes)
+      c.lanes = 2;
+    else
+      c.lanes = 4;
+    if (n <= 2) c.lanes = 1;
+  }
+  if (c.threads == 0) c.threads = 128;
+  return c;
+}
+
+}  // namespace tzg

@@ -1,0 +1,184 @@
+// Device building blocks of the batched eigenvalue-only ZGEEV path for sm_103a.
+//
+// Execution model (GB300): FP64 runs at ~2 lane-FMAs per clock per SM and a
+// warp instruction costs the same whether 1 or 32 lanes are active. The
+// kernels therefore give every matrix to a small "lane group" of L = 1, 2 or
+// 4 lanes of one warp (32/L matrices per warp), so that all 32 lanes do
+// useful FP64 work, and they keep FP64 instruction count minimal:
+//   * Householder Hessenberg reduction with v[0] = 1 and a real tau
+//     (replaces tokura_zgehrd_MWB_kernel.cuh:51-287 of the reference),
+//   * single-shift complex QR with complex Givens rotations (12 FP64 ops per
+//     element pair), Wilkinson shifts, ad hoc shifts and the Ahues-Tisseur
+//     deflation test (replaces tokura_zhseqr_MWB_kernel.cuh:221-791).
+//
+// Data layout: each warp owns one "tile" of up to 32/L matrices, staged
+// from the caller's column-major A into the caller's workspace in
+// tile-interleaved order: element (r, c) of matrix slot t of a tile of
+// width tw sits at tile[(c*n + r)*tw + t]. A warp load of the same element
+// of all its matrices is one contiguous 16*tw-byte segment.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace tzg {
+
+constexpr int kMaxN = 64;
+// LAPACK-style constants (double precision): ulp = 2^-52, safe minimum = 2^-1022.
+constexpr double kUlp = 2.220446049250313080847e-16;
+constexpr double kSafeMin = 2.225073858507201383090e-308;
+// Ad hoc shift period and weight (single-shift QR practice, LAPACK zlahqr).
+constexpr int kExceptionalPeriod = 10;
+constexpr double kExceptionalWeight = 0.75;
+
+__device__ __forceinline__ double cabs1(double2 z) { return fabs(z.x) + fabs(z.y); }
+__device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ double2 cmul(double2 a, double2 b) {
+  return make_double2(fma(a.x, b.x, -a.y * b.y), fma(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
+
+// Robust complex division p / q (Smith's method).
+__device__ __forceinline__ double2 cdiv(double2 p, double2 q) {
+  if (fabs(q.x) >= fabs(q.y)) {
+    if (q.x == 0.0) return make_double2(p.x / q.x, p.y / q.x);  // q == 0: inf/nan as IEEE says
+    double r = q.y / q.x;
+    double d = 1.0 / fma(q.y, r, q.x);
+    return make_double2(fma(p.y, r, p.x) * d, fma(-p.x, r, p.y) * d);
+  } else {
+    double r = q.x / q.y;
+    double d = 1.0 / fma(q.x, r, q.y);
+    return make_double2(fma(p.x, r, p.y) * d, fma(p.y, r, -p.x) * d);
+  }
+}
+
+// Principal complex square root, computed from |z| without overflow for the
+// magnitudes that occur here (entries are pre-scaled to ~1).
+__device__ __forceinline__ double2 csqrt_(double2 z) {
+  double m = hypot(z.x, z.y);
+  if (m == 0.0) return make_double2(0.0, 0.0);
+  double t = sqrt(0.5 * (m + fabs(z.x)));
+  double h = z.y / (2.0 * t);
+  if (z.x >= 0.0) return make_double2(t, h);
+  return make_double2(fabs(h), copysign(t, z.y));
+}
+
+// Biased exponent field of |x| (0 for zero/denormal, 2047 for inf/nan).
+__device__ __forceinline__ int dexp_field(double x) {
+  return (__double2hiint(x) >> 20) & 0x7ff;
+}
+// 2^e as a double for e in the normal range.
+__device__ __forceinline__ double pow2(int e) { return __hiloint2double((e + 1023) << 20, 0); }
+
+// Lane group of L consecutive lanes of one warp cooperating on one matrix.
+template <int L>
+struct Group {
+  unsigned mask;
+  int rank;
+  __device__ __forceinline__ Group() {
+    const int lane = threadIdx.x & 31;
+    rank = lane & (L - 1);
+    mask = (L == 32) ? 0xffffffffu : (((1u << L) - 1u) << (lane & ~(L - 1)));
+  }
+  __device__ __forceinline__ void sync() const {
+    if (L > 1) __syncwarp(mask);
+  }
+  // Butterfly reductions: every lane ends with the bitwise-identical value.
+  __device__ __forceinline__ double sum(double v) const {
+#pragma unroll
+    for (int o = L / 2; o > 0; o >>= 1) v += __shfl_xor_sync(mask, v, o);
+    return v;
+  }
+  __device__ __forceinline__ int imax(int v) const {
+#pragma unroll
+    for (int o = L / 2; o > 0; o >>= 1) v = max(v, __shfl_xor_sync(mask, v, o));
+    return v;
+  }
+  __device__ __forceinline__ int ior(int v) const {
+#pragma unroll
+    for (int o = L / 2; o > 0; o >>= 1) v |= __shfl_xor_sync(mask, v, o);
+    return v;
+  }
+};
+
+// View of one matrix inside an interleaved tile: element (r, c) at p[(c*n + r)*rs].
+struct MatView {
+  double2* p;
+  int n;
+  int rs;  // stride between consecutive rows (= tile width)
+  __device__ __forceinline__ double2* at(int r, int c) const { return p + (c * n + r) * rs; }
+};
+
+// Complex Givens rotation G = [c s; -conj(s) c] (c real) with G * [x; y] = [rr; 0].
+// The matrix is pre-scaled so |x|,|y| <= ~2^7; if |x|^2 * (|x|^2+|y|^2) underflows
+// then x is below 2^-250 relative to the matrix and is treated as zero.
+struct Rot {
+  double c;
+  double2 s;
+};
+__device__ __forceinline__ Rot make_rot(double2 x, double2 y, double2& rr) {
+  Rot g;
+  const double p = fma(x.x, x.x, x.y * x.y);
+  const double q = fma(y.x, y.x, y.y * y.y);
+  const double nn = p + q;
+  const double pn = p * nn;
+  if (q == 0.0) {  // nothing to annihilate (also covers x = y = 0)
+    g.c = 1.0;
+    g.s = make_double2(0.0, 0.0);
+    rr = x;
+  } else if (pn < 1e-290) {  // x negligible: swap-like rotation
+    const double rq = rsqrt(q);
+    g.c = 0.0;
+    g.s = make_double2(y.x * rq, -y.y * rq);  // conj(y)/|y|
+    rr = make_double2(q * rq, 0.0);          // |y|
+  } else {
+    const double R = rsqrt(pn);  // 1/(|x| * N)
+    g.c = p * R;                 // |x| / N
+    // s = x * conj(y) * R
+    const double2 xy = make_double2(fma(x.x, y.x, x.y * y.y), fma(x.y, y.x, -x.x * y.y));
+    g.s = make_double2(xy.x * R, xy.y * R);
+    const double f = nn * R;  // N / |x|
+    rr = make_double2(x.x * f, x.y * f);
+  }
+  return g;
+}
+
+// Left application to a row pair: [a; b] <- G [a; b].
+__device__ __forceinline__ void rot_left(const Rot& g, double2& a, double2& b) {
+  const double2 a0 = a, b0 = b;
+  a.x = fma(g.c, a0.x, fma(g.s.x, b0.x, -g.s.y * b0.y));
+  a.y = fma(g.c, a0.y, fma(g.s.x, b0.y, g.s.y * b0.x));
+  b.x = fma(g.c, b0.x, -fma(g.s.x, a0.x, g.s.y * a0.y));
+  b.y = fma(g.c, b0.y, -fma(g.s.x, a0.y, -g.s.y * a0.x));
+}
+// Right application to a column pair: [a b] <- [a b] G^H.
+__device__ __forceinline__ void rot_right(const Rot& g, double2& a, double2& b) {
+  const double2 a0 = a, b0 = b;
+  // a' = c a + conj(s) b ; b' = c b - s a
+  a.x = fma(g.c, a0.x, fma(g.s.x, b0.x, g.s.y * b0.y));
+  a.y = fma(g.c, a0.y, fma(g.s.x, b0.y, -g.s.y * b0.x));
+  b.x = fma(g.c, b0.x, -fma(g.s.x, a0.x, -g.s.y * a0.y));
+  b.y = fma(g.c, b0.y, -fma(g.s.x, a0.y, g.s.y * a0.x));
+}
+
+// Eigenvalue of [a b; c d] closest to d (Wilkinson shift), in a scaled,
+// cancellation-free form: d - bc / (x + sqrt(x^2 + bc)), x = (a - d)/2,
+// with the root's sign chosen so that |x + sqrt(.)| is maximal.
+__device__ __forceinline__ double2 wilkinson_shift(double2 a, double2 b, double2 c, double2 d) {
+  const double2 bc = cmul(b, c);
+  if (bc.x == 0.0 && bc.y == 0.0) return d;
+  const double2 x = make_double2(0.5 * (a.x - d.x), 0.5 * (a.y - d.y));
+  double sc = fmax(cabs1(x), sqrt(cabs1(bc)));
+  const double is = 1.0 / sc;
+  const double2 xs = cscale(x, is);
+  const double2 bcs = cscale(bc, is * is);
+  double2 y = csqrt_(cadd(cmul(xs, xs), bcs));
+  if (fma(xs.x, y.x, xs.y * y.y) < 0.0) y = make_double2(-y.x, -y.y);
+  const double2 den = cadd(xs, y);
+  if (den.x == 0.0 && den.y == 0.0) return d;
+  const double2 corr = cdiv(bcs, den);  // scaled by 1/sc
+  return make_double2(d.x - corr.x * sc, d.y - corr.y * sc);
+}
+
+}  // namespace tzg

@@ -1,0 +1,24 @@
+// Host-side internals shared by the C-ABI layer and the kernel launchers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+namespace tzg {
+
+// Launch shape of the plain (uniform-n) forward kernel for one n.
+struct PlainConfig {
+  int lanes;            // lanes per matrix: 1, 2 or 4
+  int threads;          // threads per block (multiple of 32)
+};
+
+// Iteration cap per eigenvalue: LAPACK's rule 30*max(10, n) unless overridden.
+inline int default_itmax(int n) { return 30 * (n > 10 ? n : 10); }
+
+// Launches the fused stage + Hessenberg + QR kernel on `stream`.
+// `work` must hold 16*n*n*batch bytes (tile-interleaved copy of A).
+cudaError_t launch_plain(const PlainConfig& cfg, int n, int batch, const double2* A, double2* eig,
+                         double2* work, char* flag, int itmax, cudaStream_t stream);
+
+}  // namespace tzg

@@ -1,0 +1,279 @@
+// Per-matrix algorithm executed by one lane group (L lanes of a warp).
+//
+// The functions here are the hot path: stage + scale, Householder
+// Hessenberg reduction, single-shift complex QR to Schur diagonal, and the
+// eigenvalue/flag write-out. Every lane of a group runs the same control
+// flow (all decisions come from bitwise-identical group reductions), so the
+// only divergence inside a warp is between different matrices.
+#pragma once
+
+#include "zgeev_device.cuh"
+
+namespace tzg {
+
+// Result codes of the per-matrix solve, stored in flag[] (0 = converged,
+// which is the reference's contract, tokura_zhseqr_MWB_kernel.cuh:768-776).
+enum : int { kConverged = 0, kNotConverged = 1, kNonFinite = 2 };
+
+// Stage matrix `slot` of a tile from column-major `src` (n*n elements) into
+// the tile-interleaved view, scaling by an exact power of two when the
+// largest |Re|,|Im| lies outside [2^-60, 2^60] (zgeev's pre-scaling,
+// done exactly). Returns the applied exponent shift (eigenvalues are
+// multiplied by 2^shift on output), or sets `nonfinite`.
+template <int L>
+__device__ __forceinline__ int stage_and_scale(const double2* __restrict__ src, const MatView& M,
+                                               const Group<L>& G, bool& nonfinite, bool& zero) {
+  const int nn = M.n * M.n;
+  int emax = 0;
+  for (int e = G.rank; e < nn; e += L) {
+    const double2 z = src[e];
+    emax = max(emax, max(dexp_field(z.x), dexp_field(z.y)));
+  }
+  emax = G.imax(emax);
+  nonfinite = (emax == 0x7ff);
+  zero = (emax == 0);
+  int shift = 0;
+  if (!nonfinite && !zero) {
+    const int top = emax - 1023;  // |largest| in [2^top, 2^(top+1))
+    if (top > 60 || top < -60) shift = top;
+  }
+  if (shift == 0) {
+    for (int e = G.rank; e < nn; e += L) M.p[e * M.rs] = src[e];
+  } else {
+    const double sc = pow2(-shift);
+    for (int e = G.rank; e < nn; e += L) {
+      const double2 z = src[e];
+      M.p[e * M.rs] = make_double2(z.x * sc, z.y * sc);
+    }
+  }
+  G.sync();
+  return shift;
+}
+
+// Householder reduction to upper Hessenberg form, in place. The reflector for
+// column r is P = I - tau v v^H with v[0] = 1, tau real, stored below the
+// subdiagonal of column r (v[1..]). Algorithmic FP64 work ~ (20/3) n^3 ops.
+template <int L>
+__device__ void hessenberg(const MatView& M, const Group<L>& G) {
+  const int n = M.n;
+  const int rs = M.rs;
+  const int cs = n * rs;  // column stride
+  for (int r = 0; r + 2 < n; ++r) {
+    const int m = n - r - 1;  // x = H[r+1 .. n-1, r]
+    double2* x = M.at(r + 1, r);
+    double s2 = 0.0;
+    for (int i = 1 + G.rank; i < m; i += L) {
+      const double2 z = x[i * rs];
+      s2 = fma(z.x, z.x, fma(z.y, z.y, s2));
+    }
+    s2 = G.sum(s2);
+    if (s2 == 0.0) continue;  // column already in Hessenberg form (group-uniform)
+    const double2 x0 = x[0];
+    const double a0sq = fma(x0.x, x0.x, x0.y * x0.y);
+    const double tot = a0sq + s2;
+    const double rxn = rsqrt(tot);  // 1/||x||
+    const double xn = tot * rxn;    // ||x||
+    double tau;
+    double2 cg;     // v[i] = x[i] * cg
+    double2 alpha;  // new subdiagonal entry
+    if (a0sq > 0.0) {
+      const double ra0 = rsqrt(a0sq);
+      const double a0 = a0sq * ra0;        // |x0|
+      const double d = a0 + xn;            // |u0|
+      const double ig = ra0 / d;           // 1/(|x0| (|x0| + ||x||))
+      cg = make_double2(x0.x * ig, -x0.y * ig);
+      const double f = -xn * ra0;          // alpha = -x0 ||x|| / |x0|
+      alpha = make_double2(x0.x * f, x0.y * f);
+      tau = d * rxn;                       // (|x0| + ||x||)/||x||
+    } else {
+      cg = make_double2(rxn, 0.0);
+      alpha = make_double2(-xn, 0.0);
+      tau = 1.0;
+    }
+    for (int i = 1 + G.rank; i < m; i += L) x[i * rs] = cmul(x[i * rs], cg);
+    G.sync();
+    if (G.rank == 0) x[0] = alpha;
+    // Left update: H[r+1:, c] -= tau v (v^H H[r+1:, c]) for c = r+1 .. n-1.
+    for (int c = r + 1 + G.rank; c < n; c += L) {
+      double2* col = M.at(r + 1, c);
+      double2 w = col[0];
+      for (int i = 1; i < m; ++i) {
+        const double2 v = x[i * rs];
+        const double2 a = col[i * rs];
+        w.x = fma(v.x, a.x, fma(v.y, a.y, w.x));
+        w.y = fma(v.x, a.y, fma(-v.y, a.x, w.y));
+      }
+      const double2 t = make_double2(w.x * tau, w.y * tau);
+      col[0] = csub(col[0], t);
+      for (int i = 1; i < m; ++i) {
+        const double2 v = x[i * rs];
+        double2 a = col[i * rs];
+        a.x = fma(-v.x, t.x, fma(v.y, t.y, a.x));
+        a.y = fma(-v.x, t.y, fma(-v.y, t.x, a.y));
+        col[i * rs] = a;
+      }
+    }
+    G.sync();
+    // Right update: H[q, r+1:] -= tau (H[q, r+1:] v) v^H for every row q.
+    for (int q = G.rank; q < n; q += L) {
+      double2* row = M.at(q, r + 1);
+      double2 y = row[0];
+      for (int i = 1; i < m; ++i) {
+        const double2 v = x[i * rs];
+        const double2 a = row[i * cs];
+        y.x = fma(a.x, v.x, fma(-a.y, v.y, y.x));
+        y.y = fma(a.x, v.y, fma(a.y, v.x, y.y));
+      }
+      const double2 t = make_double2(y.x * tau, y.y * tau);
+      row[0] = csub(row[0], t);
+      for (int i = 1; i < m; ++i) {
+        const double2 v = x[i * rs];
+        double2 a = row[i * cs];
+        // a -= t conj(v)
+        a.x = fma(-t.x, v.x, fma(-t.y, v.y, a.x));
+        a.y = fma(-t.y, v.x, fma(t.x, v.y, a.y));
+        row[i * cs] = a;
+      }
+    }
+    G.sync();
+  }
+}
+
+// Deflation test for subdiagonal entry k (k >= 1) of the active block [lo, hi]:
+// negligible by the Ahues-Tisseur criterion (LAPACK Working Note 122), with
+// smlnum guarding underflow.
+__device__ __forceinline__ bool negligible_subdiag(const MatView& M, int k, int lo, int hi, double smlnum) {
+  const double2 hk = *M.at(k, k - 1);
+  const double h1 = cabs1(hk);
+  if (h1 <= smlnum) return true;
+  const double2 dkk = *M.at(k, k);
+  const double2 dk1 = *M.at(k - 1, k - 1);
+  double tst = cabs1(dk1) + cabs1(dkk);
+  if (tst == 0.0) {
+    if (k - 2 >= lo) tst += cabs1(*M.at(k - 1, k - 2));
+    if (k + 1 <= hi) tst += cabs1(*M.at(k + 1, k));
+  }
+  if (h1 > kUlp * tst) return false;
+  const double2 up = *M.at(k - 1, k);
+  const double hu = cabs1(up);
+  const double ab = fmax(h1, hu), ba = fmin(h1, hu);
+  const double dd = cabs1(csub(dk1, dkk));
+  const double d1 = cabs1(dkk);
+  const double aa = fmax(d1, dd), bb = fmin(d1, dd);
+  const double s = aa + ab;
+  return ba * (ab / s) <= fmax(smlnum, kUlp * (bb * (aa / s)));
+}
+
+// Single-shift complex QR on the Hessenberg matrix (eigenvalues only), from
+// the bottom up. On return eig_out[i] holds the i-th Schur diagonal entry
+// (times 2^shift). Returns kConverged or kNotConverged. The per-eigenvalue
+// sweep cap defaults to LAPACK's 30*max(10, n).
+template <int L>
+__device__ int qr_eigenvalues(const MatView& M, const Group<L>& G, double2* __restrict__ eig_out, int shift,
+                              int itmax) {
+  const int n = M.n;
+  const int rs = M.rs;
+  const int cs = n * rs;
+  const double smlnum = kSafeMin * ((double)n / kUlp);
+  const double unscale = (shift != 0) ? pow2(shift) : 1.0;
+  int status = kConverged;
+  int i = n - 1;
+  int kdefl = 0;
+  while (i >= 0) {
+    int lo = 0;
+    bool done = false;
+    for (int its = 0; its <= itmax; ++its) {
+      // Locate the lowest negligible subdiagonal in (lo, i]; lanes scan
+      // interleaved k's from the bottom and the group keeps the largest hit.
+      int hit = lo;
+      for (int k = i - G.rank; k > lo; k -= L) {
+        if (negligible_subdiag(M, k, lo, i, smlnum)) {
+          hit = k;
+          break;
+        }
+      }
+      lo = G.imax(hit);
+      if (lo >= i) {
+        done = true;
+        break;
+      }
+      ++kdefl;
+      // Shift selection.
+      double2 sigma;
+      if (kdefl % (2 * kExceptionalPeriod) == 0) {
+        const double2 d = *M.at(i, i);
+        sigma = make_double2(d.x + kExceptionalWeight * cabs1(*M.at(i, i - 1)), d.y);
+      } else if (kdefl % kExceptionalPeriod == 0) {
+        const double2 d = *M.at(lo, lo);
+        sigma = make_double2(d.x + kExceptionalWeight * cabs1(*M.at(lo + 1, lo)), d.y);
+      } else {
+        sigma = wilkinson_shift(*M.at(i - 1, i - 1), *M.at(i - 1, i), *M.at(i, i - 1), *M.at(i, i));
+      }
+      // One implicit single-shift sweep over the active block [lo, i].
+      for (int j = lo; j < i; ++j) {
+        double2 x, y, rr;
+        if (j == lo) {
+          x = csub(*M.at(lo, lo), sigma);
+          y = *M.at(lo + 1, lo);
+        } else {
+          x = *M.at(j, j - 1);
+          y = *M.at(j + 1, j - 1);
+        }
+        const Rot g = make_rot(x, y, rr);
+        G.sync();  // all lanes have read the bulge before it is overwritten
+        if (j > lo && G.rank == 0) *M.at(j, j - 1) = rr;
+        // Left: rows (j, j+1), columns j .. i.
+        {
+          double2* pc = M.at(j, j + G.rank);
+          for (int c = j + G.rank; c <= i; c += L, pc += L * cs) {
+            double2 a = pc[0], b = pc[rs];
+            rot_left(g, a, b);
+            pc[0] = a;
+            pc[rs] = b;
+          }
+        }
+        G.sync();
+        // Right: columns (j, j+1), rows lo .. min(j+2, i); row j+2 holds the
+        // new bulge (its column-j entry is zero before the rotation).
+        {
+          const int qend = min(j + 1, i);
+          double2* pr = M.at(lo + G.rank, j);
+          for (int q = lo + G.rank; q <= qend; q += L, pr += L * rs) {
+            double2 a = pr[0], b = pr[cs];
+            rot_right(g, a, b);
+            pr[0] = a;
+            pr[cs] = b;
+          }
+          if (j + 2 <= i && G.rank == ((j + 2 - lo) & (L - 1))) {
+            double2* pb = M.at(j + 2, j);
+            const double2 b = pb[cs];
+            // a' = conj(s) b ; b' = c b
+            pb[0] = make_double2(fma(g.s.x, b.x, g.s.y * b.y), fma(g.s.x, b.y, -g.s.y * b.x));
+            pb[cs] = make_double2(g.c * b.x, g.c * b.y);
+          }
+        }
+        G.sync();
+      }
+    }
+    if (!done) {
+      status = kNotConverged;
+      break;
+    }
+    if (G.rank == 0) {
+      const double2 d = *M.at(i, i);
+      eig_out[i] = make_double2(d.x * unscale, d.y * unscale);
+    }
+    kdefl = 0;
+    i = lo - 1;
+  }
+  if (status != kConverged && G.rank == 0) {
+    // Unconverged positions 0..i carry their current diagonal entries.
+    for (int k = 0; k <= i; ++k) {
+      const double2 d = *M.at(k, k);
+      eig_out[k] = make_double2(d.x * unscale, d.y * unscale);
+    }
+  }
+  return status;
+}
+
+}  // namespace tzg

@@ -1,0 +1,69 @@
+// Plain batched eigenvalue-only ZGEEV for a uniform matrix order n (1..64).
+//
+// One kernel replaces the reference's three stages (layout transpose,
+// tokura_zgehrd_normal_MWB_kernel at tokura_zgehrd_MWB_kernel.cuh:159-287 and
+// tokura_zhseqr_normal_MWB_kernel at tokura_zhseqr_MWB_kernel.cuh:611-791):
+// each warp stages its tile of 32/L matrices into the workspace, reduces
+// them to Hessenberg form and runs single-shift QR, then writes the
+// eigenvalues straight to eigenvalues[i + j*n] and flag[j].
+#include "zgeev_internal.h"
+#include "zgeev_lane.cuh"
+
+namespace tzg {
+
+template <int L>
+__global__ void __launch_bounds__(128) zgeev_plain_kernel(int n, int batch, const double2* __restrict__ A,
+                                                           double2* __restrict__ eig, double2* __restrict__ work,
+                                                           char* __restrict__ flag, int itmax) {
+  constexpr int TW = 32 / L;
+  const int lane = threadIdx.x & 31;
+  const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long g0 = warp * TW;
+  if (g0 >= batch) return;  // warp-uniform
+  const int tw = (int)min((long long)TW, (long long)batch - g0);
+  const int slot = lane / L;
+  if (slot >= tw) return;  // whole lane groups leave together; no warp-wide barriers follow
+  const Group<L> G;
+  const long long nn = (long long)n * n;
+  const long long j = g0 + slot;
+  MatView M{work + g0 * nn + slot, n, tw};
+
+  bool nonfinite, zero;
+  const int shift = stage_and_scale<L>(A + j * nn, M, G, nonfinite, zero);
+  double2* ev = eig + j * n;
+  if (nonfinite || zero) {
+    const double v = nonfinite ? __longlong_as_double(0x7ff8000000000000LL) : 0.0;
+    for (int i = G.rank; i < n; i += L) ev[i] = make_double2(v, v);
+    if (G.rank == 0) flag[j] = (char)(nonfinite ? kNonFinite : kConverged);
+    return;
+  }
+  hessenberg<L>(M, G);
+  const int status = qr_eigenvalues<L>(M, G, ev, shift, itmax);
+  if (G.rank == 0) flag[j] = (char)status;
+}
+
+cudaError_t launch_plain(const PlainConfig& cfg, int n, int batch, const double2* A, double2* eig, double2* work,
+                         char* flag, int itmax, cudaStream_t stream) {
+  const int L = cfg.lanes;
+  const int tw = 32 / L;
+  const long long warps = ((long long)batch + tw - 1) / tw;
+  const int threads = 128;
+  const long long blocks = (warps * 32 + threads - 1) / threads;
+  if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
+  switch (L) {
+    case 1:
+      zgeev_plain_kernel<1><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, eig, work, flag, itmax);
+      break;
+    case 2:
+      zgeev_plain_kernel<2><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, eig, work, flag, itmax);
+      break;
+    case 4:
+      zgeev_plain_kernel<4><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, eig, work, flag, itmax);
+      break;
+    default:
+      return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+}  // namespace tzg
