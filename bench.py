@@ -1,0 +1,399 @@
+"""Benchmark of the batched eigenvalue-only ZGEEV path on GB300.
+
+Default workload (one "step"): one call of the plain entry point
+``tokura_zgeev_batched_gpu`` on 65,536 complex128 64x64 matrices
+(4 GiB, Re/Im i.i.d. N(0,1), fixed seed) — the n=64 case of the size sweep,
+the order at which the throughput target is stated. Inputs are resident in
+HBM for ``value``; ``e2e`` times the same call with the input copied from
+pinned host memory and the eigenvalues/flags copied back inside every step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+``--impl reference`` times the reference's CPU comparison path (LAPACK zgeev
+per matrix over all host cores, stream_test_with_MKL/get_eig_MKL.c:27-47) on
+a bounded sample of the same workload. Under torchrun every rank processes its
+own batch (weak scaling, no collective on the data path); rank 0 prints the
+JSON line with the max time over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "matrices/s eigvals (n=32,64; ragged 1-64), fwd+bwd matrices/s, % FP64 peak"
+N = 64
+BATCH = (4 << 30) // (16 * N * N)  # 65,536 matrices = 4 GiB of input
+SEED = 20261203
+SWEEP_NS = (4, 8, 16, 32, 48)
+
+
+def flops_per_matrix(n: int) -> float:
+    """Algorithmic work convention: 40 n^3 real FP64 flops per matrix (Hessenberg + QR, complex)."""
+    return 40.0 * n ** 3
+
+
+def bytes_per_matrix(n: int) -> int:
+    return 16 * n * n + 16 * n + 1
+
+
+# ----------------------------------------------------------------------------- helpers
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks/throttle reasons in the background."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id: str | None):
+        self.proc = None
+        self.lines: list[str] = []
+        cmd = ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"]
+        if gpu_id:
+            cmd += ["-i", gpu_id]
+        try:
+            self.proc = subprocess.Popen(cmd, stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict | None:
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, power, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+                power.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "samples": len(sm),
+                "power_w_max": max(power), "reasons": sorted(reasons)}
+
+
+def gpu_uuid(dev) -> str | None:
+    import torch
+
+    try:
+        u = str(torch.cuda.get_device_properties(dev).uuid)
+        return u if u.startswith("GPU-") else "GPU-" + u
+    except Exception:
+        return None
+
+
+def read_profile_traffic() -> dict | None:
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return None
+
+
+def cpu_baseline(n: int, seconds: float = 8.0) -> dict:
+    """LAPACK zgeev per matrix over all host cores on a bounded sample of the workload."""
+    import numpy as np
+
+    from oracle import lapack_oracle as lo
+    from tokura_zgeev_batched_gb300 import workloads
+
+    threads = lo.default_threads()
+    probe = workloads.gaussian(max(threads * 4, 64), n, seed=SEED + 99)
+    _, _, t = lo.zgeev(probe, threads)
+    rate = probe.shape[0] / max(t, 1e-6)
+    count = int(min(max(rate * seconds, threads * 8), 200000))
+    sample = workloads.gaussian(count, n, seed=SEED + 100)
+    _, info, t = lo.zgeev(sample, threads)
+    return {"value": count / t, "unit": "matrices/s", "cores": threads, "kind": "port",
+            "sample": f"{count} complex Gaussian {n}x{n} matrices (seeded), LAPACK zgeev('N','N') from scipy's "
+                      f"OpenBLAS 0.3.34, one call per matrix, {threads} threads, {t:.2f} s",
+            "lapack_info_nonzero": int(np.count_nonzero(info))}
+
+
+# ----------------------------------------------------------------------------- reference arm
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    import numpy as np
+
+    from oracle import lapack_oracle as lo
+    from tokura_zgeev_batched_gb300 import workloads
+
+    threads = lo.default_threads()
+    sample_n = max(threads * 32, 256)
+    mats = workloads.gaussian(sample_n, N, seed=SEED + 7)
+    for _ in range(args.warmup):
+        lo.zgeev(mats[: threads * 4], threads)
+    times = []
+    for _ in range(args.steps):
+        _, info, t = lo.zgeev(mats, threads)
+        times.append(t)
+    total = sum(times)
+    value = sample_n * args.steps / total
+    out = {
+        "metric": METRIC, "value": value, "unit": "matrices/s", "impl": "reference",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "c128 (f64)", "data": "synthetic",
+        "config": {"workload": f"plain zgeev eigenvalues, n={N}, complex Gaussian; each step a {sample_n}-matrix "
+                               f"sample of the {BATCH}-matrix batch", "n": N, "batch": sample_n},
+        "cpu_baseline": {"value": value, "unit": "matrices/s", "cores": threads, "kind": "port",
+                         "sample": f"{sample_n} matrices per step, LAPACK zgeev('N','N') (scipy's OpenBLAS "
+                                   f"0.3.34) over {threads} threads; the reference's own CPU path "
+                                   f"(get_eig_MKL.c) needs MKL, which is absent"},
+        "e2e": {"value": value, "unit": "matrices/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "lapack_info_nonzero": int(np.count_nonzero(info)),
+    }
+    print(json.dumps(out), flush=True)
+
+
+# ----------------------------------------------------------------------------- our arm
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    from tokura_zgeev_batched_gb300 import api, build, workloads
+
+    ws, rank, local = dist_env()
+    dist = None
+    if ws > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    if rank == 0:
+        build.build()
+    if dist is not None:
+        dist.barrier()
+    api.lib()
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    peak = api.probe_fp64_peak(dev)
+    h = api.Handle()
+    stream = torch.cuda.current_stream(dev)
+    s = stream.cuda_stream
+
+    def alloc(n, batch, gen="gaussian", seed=SEED):
+        A = workloads.TORCH_GENERATORS[gen](batch, n, seed=seed + 1000 * rank, device=str(dev))
+        eig = torch.empty(batch, n, dtype=torch.complex128, device=dev)
+        flag = torch.empty(batch, dtype=torch.int8, device=dev)
+        work = torch.empty(api.tokura_get_zgeeveigenvaluesgetworspacesize(n, batch), dtype=torch.uint8, device=dev)
+        return A, eig, flag, work
+
+    def call(n, batch, A, eig, flag, work):
+        st = api.tokura_zgeev_batched_gpu(h, n, batch, A.data_ptr(), eig.data_ptr(), work.data_ptr(),
+                                          flag.data_ptr(), s)
+        if st != 0:
+            raise RuntimeError(f"tokura_zgeev_batched_gpu returned {st}")
+
+    # ---- main workload: n = 64, 4 GiB
+    A, eig, flag, work = alloc(N, BATCH)
+    for _ in range(args.warmup):
+        call(N, BATCH, A, eig, flag, work)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(gpu_uuid(dev))
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    barrier()
+    torch.cuda.synchronize()
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for k in range(args.steps):
+        ev[k][0].record(stream)
+        call(N, BATCH, A, eig, flag, work)
+        ev[k][1].record(stream)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clocks = sampler.stop()
+    ms_total = t0.elapsed_time(t1)
+    kern_ms = [a.elapsed_time(b) for a, b in ev]
+    if dist is not None:
+        tt = torch.tensor([ms_total], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        ms_total = float(tt.item())
+    ms_step = ms_total / args.steps
+    value = ws * BATCH / (ms_step * 1e-3)
+    flagged = int((flag != 0).sum().item())
+
+    # Parity spot check of the timed output against LAPACK (rank 0, outside timing).
+    parity = None
+    if rank == 0 and not args.no_check:
+        from oracle import lapack_oracle as lo
+
+        idx = torch.arange(0, BATCH, BATCH // 256, device=dev)[:256]
+        rep = lo.parity_report(A[idx].cpu().numpy(), eig[idx].cpu().numpy(), flag[idx].cpu().numpy())
+        parity = {"checked": 256, "max_rel_err_fro": rep["max_rel_err"], "flag_mismatch": rep["flag_mismatch"],
+                  "max_rel_err_fro_cond_le_1e3": rep.get("max_rel_err_well")}
+
+    kern_avg = statistics.mean(kern_ms)
+    achieved = flops_per_matrix(N) * BATCH / (kern_avg * 1e-3)
+    prof = read_profile_traffic()
+    traffic = None
+    if prof and prof.get("n") == N:
+        traffic = prof.get("dram_bytes_per_launch")
+    roofline = {
+        "bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
+        "frac": achieved / peak, "traffic": traffic,
+        "peak_source": "FP64 FMA-loop probe run in this process (MEASURED_PEAKS.json has no FP64 figure)",
+        "algorithmic": f"40*n^3 flops and 16*n^2+16*n+1 bytes per matrix x {BATCH} matrices per launch",
+        "kernel_ms_avg": kern_avg,
+    }
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            hbm_peak = json.load(f).get("hbm_gbs")
+    except (OSError, ValueError):
+        hbm_peak = None
+    alg_gbs = bytes_per_matrix(N) * BATCH / (kern_avg * 1e-3) / 1e9
+    roofline["hbm"] = {"achieved": alg_gbs, "peak": hbm_peak, "unit": "GB/s",
+                       "frac": (alg_gbs / hbm_peak) if hbm_peak else None}
+
+    # ---- end to end: host buffers through the public API, copies inside every step
+    e2e = None
+    if not args.no_e2e:
+        A_host = torch.empty(A.shape, dtype=A.dtype, pin_memory=True)
+        A_host.copy_(A)
+        eig_host = torch.empty(eig.shape, dtype=eig.dtype, pin_memory=True)
+        flag_host = torch.empty(flag.shape, dtype=flag.dtype, pin_memory=True)
+        torch.cuda.synchronize()
+
+        def e2e_step():
+            A.copy_(A_host, non_blocking=True)
+            call(N, BATCH, A, eig, flag, work)
+            eig_host.copy_(eig, non_blocking=True)
+            flag_host.copy_(flag, non_blocking=True)
+
+        for _ in range(max(1, args.warmup)):
+            e2e_step()
+        torch.cuda.synchronize()
+        barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            e2e_step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+        e_ms = e0.elapsed_time(e1) / args.steps
+        if dist is not None:
+            tt = torch.tensor([e_ms], device=dev)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            e_ms = float(tt.item())
+        e2e = {"value": ws * BATCH / (e_ms * 1e-3), "unit": "matrices/s",
+               "h2d_bytes_per_step": A_host.numel() * 16,
+               "d2h_bytes_per_step": eig_host.numel() * 16 + flag_host.numel(),
+               "ms_per_step": e_ms}
+        del A_host, eig_host, flag_host
+    del A, eig, flag, work
+    torch.cuda.empty_cache()
+
+    # ---- size sweep (the other orders of the 4 GiB size-sweep configuration)
+    sweep = {}
+    if not args.no_sweep:
+        for n in SWEEP_NS:
+            batch = (4 << 30) // (16 * n * n)
+            A, eig, flag, work = alloc(n, batch)
+            call(n, batch, A, eig, flag, work)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            reps = 2
+            e0.record(stream)
+            for _ in range(reps):
+                call(n, batch, A, eig, flag, work)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            rate = batch / (ms * 1e-3)
+            sweep[str(n)] = {"batch": batch, "matrices_per_s": rate,
+                             "fp64_frac": flops_per_matrix(n) * rate / peak,
+                             "flagged": int((flag != 0).sum().item())}
+            del A, eig, flag, work
+            torch.cuda.empty_cache()
+        sweep[str(N)] = {"batch": BATCH, "matrices_per_s": value / ws, "fp64_frac": achieved / peak,
+                         "flagged": flagged}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(N)
+
+    if rank == 0:
+        out = {
+            "metric": METRIC, "value": value, "unit": "matrices/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c128 (f64)", "data": "synthetic",
+            "config": {"workload": f"plain zgeev eigenvalues (tokura_zgeev_batched_gpu), n={N}, {BATCH} complex "
+                                   f"Gaussian matrices per GPU (4 GiB), seed {SEED}",
+                       "n": N, "global_batch": ws * BATCH, "l2": "inputs (4 GiB) larger than L2",
+                       "lanes_per_matrix": h.plain_config(N, BATCH)[0]},
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
+            "gpu_launches": args.steps, "flagged": flagged, "parity_spot_check": parity, "sweep": sweep,
+        }
+        print(json.dumps(out), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-sweep", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-check", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,45 @@
+/*
+ * tokura_blas_ext.h — entry points beyond the reference's API.
+ *
+ * The reference (hirokitokura/tokura_zgeev_batched) has no counterpart for
+ * these; each comment says what it adds. All data pointers are device
+ * pointers; all calls are asynchronous on `stream` unless stated.
+ */
+#ifndef TOKURA_BLAS_EXT_GB300_H
+#define TOKURA_BLAS_EXT_GB300_H
+
+#include "tokura_blas.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Per-eigenvalue QR sweep cap used by later calls on this handle
+ * (0 restores LAPACK's rule 30*max(10, n)). A small cap forces flag[j] = 1,
+ * which the tests use to exercise the non-convergence path.
+ * Returns 0, or -1 for a NULL handle / negative cap. Configuration call:
+ * do not race it with compute calls on the same handle. */
+TOKURA_API int tokuraSetSweepCap(tokurablas_t* handle, int cap);
+
+/* Launch shape of the plain kernel for order n: lanes per matrix (1, 2 or 4;
+ * 0 = choose from the batch size) and threads per block (32..256, multiple
+ * of 32; 0 = 128). Replaces the reference's compile-time tables
+ * (include/tokura_zhseqr_parameters.h, tokura_zgeev_batched.cu:13-60).
+ * Returns 0, -1 NULL handle, -2 n out of range, -3 bad lanes, -4 bad threads. */
+TOKURA_API int tokuraSetPlainConfig(tokurablas_t* handle, int n, int lanes_per_matrix, int threads_per_block);
+
+/* The launch shape the next plain call with (n, batch_count) will use. */
+TOKURA_API int tokuraGetPlainConfig(const tokurablas_t* handle, int n, int batch_count, int* lanes_per_matrix,
+                                    int* threads_per_block);
+
+/* Measures the device's FP64 FMA throughput (FLOP/s, 2 per FMA) with a
+ * saturating FMA loop; synchronizes `stream`. scratch: >= 512*SMs doubles.
+ * Returns 0, -1 NULL pointer, -2 scratch too small, 1 CUDA failure. */
+TOKURA_API int tokura_probe_fp64_peak(double* flops_per_second, double* scratch, int scratch_doubles,
+                                      cudaStream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TOKURA_BLAS_EXT_GB300_H */

@@ -31,6 +31,14 @@ _SIGNATURES = {
         [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
          ctypes.c_void_p, ctypes.c_void_p],
     ),
+    "tokuraSetSweepCap": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "tokuraSetPlainConfig": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "tokuraGetPlainConfig": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)],
+    ),
+    "tokura_probe_fp64_peak": (
+        ctypes.c_int, [ctypes.POINTER(ctypes.c_double), ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
 }
 
 
@@ -70,6 +78,19 @@ class Handle:
     @property
     def value(self) -> int:
         return self.ptr.value
+
+    def set_sweep_cap(self, cap: int) -> int:
+        return int(lib().tokuraSetSweepCap(self.ptr, int(cap)))
+
+    def set_plain_config(self, n: int, lanes: int, threads: int) -> int:
+        return int(lib().tokuraSetPlainConfig(self.ptr, int(n), int(lanes), int(threads)))
+
+    def plain_config(self, n: int, batch: int) -> tuple[int, int]:
+        lanes, threads = ctypes.c_int(), ctypes.c_int()
+        st = lib().tokuraGetPlainConfig(self.ptr, int(n), int(batch), ctypes.byref(lanes), ctypes.byref(threads))
+        if st != 0:
+            raise ValueError(f"tokuraGetPlainConfig returned {st}")
+        return lanes.value, threads.value
 
     def close(self):
         if self.ptr is not None and self.ptr.value:
@@ -164,3 +185,18 @@ def zgeev_batched(A, handle: Handle | None = None, work=None, stream=None):
     if status != 0:
         raise RuntimeError(f"tokura_zgeev_batched_gpu returned {status}")
     return eig.reshape(*batch_shape, n), flag.reshape(batch_shape)
+
+
+def probe_fp64_peak(device=None) -> float:
+    """Measured FP64 FMA throughput of the device in FLOP/s (synchronizes)."""
+    import torch
+
+    dev = torch.device(device) if device is not None else torch.device("cuda", torch.cuda.current_device())
+    sms = torch.cuda.get_device_properties(dev).multi_processor_count
+    scratch = torch.empty(512 * sms, dtype=torch.float64, device=dev)
+    out = ctypes.c_double()
+    st = lib().tokura_probe_fp64_peak(ctypes.byref(out), scratch.data_ptr(), scratch.numel(),
+                                      torch.cuda.current_stream(dev).cuda_stream)
+    if st != 0:
+        raise RuntimeError(f"tokura_probe_fp64_peak returned {st}")
+    return out.value

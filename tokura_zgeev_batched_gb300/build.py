@@ -27,6 +27,7 @@ ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden", "--expt-relaxed-constexpr"]
 SOURCES = [
     "zgeev_plain.cu",
+    "peak_probe.cu",
     "tokura_capi.cpp",
     "compat_cxx.cpp",
 ]

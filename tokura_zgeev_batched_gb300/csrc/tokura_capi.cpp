@@ -9,7 +9,7 @@
 // the NULL-handle check happens before any dereference.
 #include <new>
 
-#include "../../include/tokura_blas.h"
+#include "../../include/tokura_blas_ext.h"
 #include "tokura_handle.h"
 #include "zgeev_internal.h"
 
@@ -57,4 +57,31 @@ extern "C" int tokura_zgeev_batched_gpu(tokurablas_t* handle, int n, int batch_c
                                             reinterpret_cast<double2*>(eigenvalues),
                                             reinterpret_cast<double2*>(work), flag, itmax, cudastream);
   return err == cudaSuccess ? 0 : 1;
+}
+
+extern "C" int tokuraSetSweepCap(tokurablas_t* handle, int cap) {
+  if (handle == nullptr || cap < 0) return -1;
+  handle->itmax_override = cap;
+  return 0;
+}
+
+extern "C" int tokuraSetPlainConfig(tokurablas_t* handle, int n, int lanes_per_matrix, int threads_per_block) {
+  if (handle == nullptr) return -1;
+  if (!(n > 0 && n <= TOKURA_ZGEEV_BATCHED_MAX_MATRIX_SIZE)) return -2;
+  if (!(lanes_per_matrix == 0 || lanes_per_matrix == 1 || lanes_per_matrix == 2 || lanes_per_matrix == 4)) return -3;
+  if (!(threads_per_block == 0 || (threads_per_block >= 32 && threads_per_block <= 256 && threads_per_block % 32 == 0)))
+    return -4;
+  handle->plain[n] = PlainConfig{lanes_per_matrix, threads_per_block};
+  return 0;
+}
+
+extern "C" int tokuraGetPlainConfig(const tokurablas_t* handle, int n, int batch_count, int* lanes_per_matrix,
+                                    int* threads_per_block) {
+  if (handle == nullptr || lanes_per_matrix == nullptr || threads_per_block == nullptr) return -1;
+  if (!(n > 0 && n <= TOKURA_ZGEEV_BATCHED_MAX_MATRIX_SIZE)) return -2;
+  if (!(batch_count > 0)) return -6;
+  const PlainConfig c = tzg::plain_config_for(handle, n, batch_count);
+  *lanes_per_matrix = c.lanes;
+  *threads_per_block = c.threads;
+  return 0;
 }

@@ -12,7 +12,7 @@
 namespace tzg {
 
 template <int L>
-__global__ void __launch_bounds__(128) zgeev_plain_kernel(int n, int batch, const double2* __restrict__ A,
+__global__ void __launch_bounds__(256) zgeev_plain_kernel(int n, int batch, const double2* __restrict__ A,
                                                            double2* __restrict__ eig, double2* __restrict__ work,
                                                            char* __restrict__ flag, int itmax) {
   constexpr int TW = 32 / L;
@@ -47,9 +47,9 @@ cudaError_t launch_plain(const PlainConfig& cfg, int n, int batch, const double2
   const int L = cfg.lanes;
   const int tw = 32 / L;
   const long long warps = ((long long)batch + tw - 1) / tw;
-  const int threads = 128;
+  const int threads = cfg.threads;
   const long long blocks = (warps * 32 + threads - 1) / threads;
-  if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
+  if (blocks > 0x7fffffffLL || threads < 32 || threads > 256 || threads % 32 != 0) return cudaErrorInvalidValue;
   switch (L) {
     case 1:
       zgeev_plain_kernel<1><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, eig, work, flag, itmax);
