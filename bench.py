@@ -36,6 +36,13 @@ SEED = 20261203
 SWEEP_NS = (4, 8, 16, 32, 48)
 
 
+def set_workload(n: int, batch: int = 0) -> None:
+    """Overrides the timed workload (used for small profiling captures)."""
+    global N, BATCH
+    N = int(n)
+    BATCH = int(batch) if batch > 0 else (4 << 30) // (16 * N * N)
+
+
 def flops_per_matrix(n: int) -> float:
     """Algorithmic work convention: 40 n^3 real FP64 flops per matrix (Hessenberg + QR, complex)."""
     return 40.0 * n ** 3
@@ -388,7 +395,10 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-check", action="store_true")
+    ap.add_argument("--n", type=int, default=N, help="matrix order of the timed workload (profiling cases)")
+    ap.add_argument("--batch", type=int, default=0, help="matrices per GPU (default: 4 GiB of input)")
     args = ap.parse_args()
+    set_workload(args.n, args.batch)
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -162,7 +162,9 @@ def parity_report(A: np.ndarray, w_test: np.ndarray, flag_test: np.ndarray, thre
     err = np.full(w_ref.shape, np.nan)
     if ok.any():
         err[ok] = matched_abs_errors(np.asarray(w_test)[ok], w_ref[ok])
-    rel = np.nanmax(err, axis=1) / fro
+    rel = np.full(A.shape[0], np.nan)
+    if ok.any():
+        rel[ok] = np.max(err[ok], axis=1) / fro[ok]
     rep = {
         "batch": int(A.shape[0]),
         "flag_mismatch": int(np.sum((info != 0) != (np.asarray(flag_test) != 0))),

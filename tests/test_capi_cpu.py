@@ -1,0 +1,120 @@
+"""C-ABI library: builds, loads, exports every declared symbol, validates arguments (no GPU needed)."""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+from tokura_zgeev_batched_gb300 import api, build
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADERS = [os.path.join(ROOT, "include", f) for f in sorted(os.listdir(os.path.join(ROOT, "include")))]
+
+
+def declared_symbols():
+    names = []
+    for h in HEADERS:
+        text = open(h).read()
+        names += re.findall(r"TOKURA_API\s+[\w\s\*]+?\b(\w+)\s*\(", text)
+    return names
+
+
+@pytest.fixture(scope="module")
+def lib():
+    return api.lib()
+
+
+def defined_dynamic_symbols():
+    out = subprocess.run(["nm", "-D", "--defined-only", build.LIB_PATH], capture_output=True, text=True, check=True)
+    return {ln.split()[-1] for ln in out.stdout.splitlines() if ln.strip()}
+
+
+def test_every_declared_symbol_is_exported(lib):
+    decl = declared_symbols()
+    assert "tokura_zgeev_batched_gpu" in decl and len(decl) >= 8
+    syms = defined_dynamic_symbols()
+    for name in decl:
+        assert name in syms, name
+        getattr(lib, name)
+
+
+def test_reference_mangled_names_exported(lib):
+    syms = defined_dynamic_symbols()
+    for mangled in (
+        "_Z12tokuraCreatePP12tokurablas_t",
+        "_Z13tokuraDestroyP12tokurablas_t",
+        "_Z42tokura_get_zgeeveigenvaluesgetworspacesizeii",
+        "_Z24tokura_zgeev_batched_gpuP12tokurablas_tiiP7double2S2_S2_PcP11CUstream_st",
+    ):
+        assert mangled in syms, mangled
+
+
+def test_python_signature_table_covers_header():
+    assert set(declared_symbols()) <= set(api.exported_symbols())
+
+
+def test_workspace_size_formula(lib):
+    ws = api.tokura_get_zgeeveigenvaluesgetworspacesize
+    assert ws(32, 10000) == 16 * 32 * 32 * 10000 + 16 * 32 * 10000
+    assert ws(1, 1) == 32
+    assert ws(64, 65536) == 16 * 64 * 64 * 65536 + 16 * 64 * 65536
+    size_max = 2 ** 64 - 1
+    assert ws(0, 5) == size_max and ws(65, 5) == size_max and ws(-3, 5) == size_max
+    assert ws(8, 0) == size_max - 1 and ws(8, -1) == size_max - 1
+
+
+def test_argument_validation_codes(lib):
+    fake = ctypes.c_void_p(0x1000)  # never dereferenced: every call below fails validation first
+    p = 0x2000
+    f = api.tokura_zgeev_batched_gpu
+    assert f(None, 8, 4, p, p, p, p, 0) == -1
+    assert f(fake, 0, 4, p, p, p, p, 0) == -2
+    assert f(fake, 65, 4, p, p, p, p, 0) == -2
+    assert f(fake, 8, 4, None, p, p, p, 0) == -3
+    assert f(fake, 8, 4, p, None, p, p, 0) == -4
+    assert f(fake, 8, 4, p, p, None, p, 0) == -5
+    assert f(fake, 8, 0, p, p, p, p, 0) == -6
+    assert f(fake, 8, -2, p, p, p, p, 0) == -6
+    assert f(fake, 8, 4, p, p, p, None, 0) == -7
+    # order of checks follows the reference (tokura_zgeev_batched.cu:237-264)
+    assert f(fake, 0, 0, None, None, None, None, 0) == -2
+
+
+def test_create_destroy_null(lib):
+    assert lib.tokuraCreate(None) == -1
+    assert lib.tokuraDestroy(None) == 0
+    assert lib.tokuraSetSweepCap(None, 3) == -1
+
+
+def test_reference_style_caller_links(tmp_path, lib):
+    """An object compiled against the reference's (C++-linkage) declarations links to this library."""
+    src = tmp_path / "caller.cpp"
+    src.write_text(
+        "#include <cuda_runtime_api.h>\n#include <cuComplex.h>\n#include <stddef.h>\n"
+        "typedef struct tokurablas_t tokurablas_t;\n"
+        "int tokuraCreate(tokurablas_t** h);\nint tokuraDestroy(tokurablas_t* h);\n"
+        "size_t tokura_get_zgeeveigenvaluesgetworspacesize(int, int);\n"
+        "int tokura_zgeev_batched_gpu(tokurablas_t*, int, int, cuDoubleComplex*, cuDoubleComplex*, cuDoubleComplex*,"
+        " char*, cudaStream_t);\n"
+        "int main() { return (int)tokura_get_zgeeveigenvaluesgetworspacesize(2, 1) == 96 ? 0 : 1; }\n"
+    )
+    exe = tmp_path / "caller"
+    cuda_inc = "/usr/local/cuda/include"
+    r = subprocess.run(["g++", str(src), "-I", cuda_inc, "-o", str(exe), build.LIB_PATH,
+                        "-Wl,-rpath," + os.path.dirname(build.LIB_PATH), "-Wl,--unresolved-symbols=ignore-in-shared-libs"],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    nm = subprocess.run(["nm", str(exe)], capture_output=True, text=True).stdout
+    assert "_Z42tokura_get_zgeeveigenvaluesgetworspacesizeii" in nm
+    run = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert run.returncode == 0
+
+
+def test_c_caller_compiles_against_header(tmp_path):
+    src = tmp_path / "c_caller.c"
+    src.write_text('#include "tokura_blas_ext.h"\nint main(void){ tokurablas_t* h = 0; (void)h;'
+                   ' return (int)(tokura_get_zgeeveigenvaluesgetworspacesize(1, 1) != 32); }\n')
+    r = subprocess.run(["gcc", "-std=c99", "-c", str(src), "-I", os.path.join(ROOT, "include"), "-I",
+                        "/usr/local/cuda/include", "-o", str(tmp_path / "c_caller.o")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr

@@ -1,0 +1,89 @@
+"""The oracle (LAPACK zgeev via oracle/cpu_zgeev.c) pinned against known answers and the golden fixtures."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import lapack_oracle as lo
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "zgeev_golden.npz")
+
+
+@pytest.fixture(scope="module")
+def golden():
+    return np.load(GOLDEN)
+
+
+def cases(g):
+    return [str(x) for x in g["names"]]
+
+
+def test_oracle_reproduces_golden(golden):
+    for name in cases(golden):
+        A = golden[f"{name}/A"]
+        w, info, _ = lo.zgeev(A, threads=2)
+        assert np.array_equal(info, golden[f"{name}/info"]), name
+        err = lo.matched_abs_errors(w, golden[f"{name}/w"])
+        scale = np.maximum(np.sqrt(np.sum(np.abs(A) ** 2, axis=(1, 2))), 1e-300)
+        assert np.all(err.max(axis=1) <= 1e-12 * scale + 1e-300) or name.startswith("jordan"), name
+
+
+def test_oracle_known_answers(golden):
+    # Exact spectra: triangular, diagonal, circulant, constructed V diag V^-1.
+    for name in cases(golden):
+        key = f"{name}/exact"
+        if key not in golden.files:
+            continue
+        A = golden[f"{name}/A"]
+        w, info, _ = lo.zgeev(A, threads=2)
+        assert (info == 0).all(), name
+        err = lo.matched_abs_errors(w, golden[key])
+        fro = np.sqrt(np.sum(np.abs(A) ** 2, axis=(1, 2)))
+        cond = 1.0 / np.maximum(golden[f"{name}/rconde"], 1e-300)
+        bound = np.where(fro > 0, fro, 1.0) * 1e-13 * np.maximum(cond.max(axis=1), 1.0)
+        if name.startswith("jordan"):
+            # defective eigenvalue: LAPACK error ~ eps^(1/n)
+            n = A.shape[-1]
+            assert err.max() <= 10 * (2.2e-16 * fro.max()) ** (1.0 / n), name
+        else:
+            assert np.all(err.max(axis=1) <= bound), (name, err.max(axis=1), bound)
+
+
+def test_matching_is_optimal():
+    rng = np.random.default_rng(0)
+    w = rng.standard_normal(8) + 1j * rng.standard_normal(8)
+    perm = rng.permutation(8)
+    e = lo.matched_abs_errors(w[perm][None] + 1e-14, w[None])
+    assert e.max() < 1e-13
+
+
+def test_parity_report_detects_errors():
+    from tokura_zgeev_batched_gb300 import workloads as wl
+
+    A = wl.gaussian(4, 6, seed=1)
+    w, info, _ = lo.zgeev(A)
+    flags = np.zeros(4, np.int8)
+    rep = lo.parity_report(A, w, flags)
+    assert rep["max_rel_err"] < 1e-14 and rep["flag_mismatch"] == 0
+    bad = w.copy()
+    bad[2, 3] += 1e-6
+    rep = lo.parity_report(A, bad, flags)
+    assert rep["max_rel_err"] > 1e-8
+    flags[1] = 1
+    rep = lo.parity_report(A, w, flags)
+    assert rep["flag_mismatch"] == 1
+
+
+def test_condition_numbers_match_eigenvector_formula():
+    import scipy.linalg as sl
+
+    from tokura_zgeev_batched_gb300 import workloads as wl
+
+    A = wl.gaussian(3, 7, seed=3)
+    w, rc, info = lo.zgeevx_rconde(A)
+    for k in range(3):
+        # The harness reads buffers column-major: it sees A[k].T
+        wk, vl, vr = sl.eig(A[k].T, left=True, right=True)
+        s = np.abs(np.sum(vl.conj() * vr, axis=0)) / (np.linalg.norm(vl, axis=0) * np.linalg.norm(vr, axis=0))
+        order = [int(np.argmin(np.abs(wk - x))) for x in w[k]]
+        assert np.allclose(rc[k], s[order], rtol=1e-8)

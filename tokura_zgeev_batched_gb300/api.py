@@ -132,6 +132,8 @@ def _ptr(h) -> int | None:
         return None
     if isinstance(h, Handle):
         return h.value
+    if isinstance(h, ctypes.c_void_p):
+        return h.value
     return int(h)
 
 
