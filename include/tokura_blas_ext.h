@@ -38,6 +38,27 @@ TOKURA_API int tokuraGetPlainConfig(const tokurablas_t* handle, int n, int batch
 TOKURA_API int tokura_probe_fp64_peak(double* flops_per_second, double* scratch, int scratch_doubles,
                                       cudaStream_t stream);
 
+/* Same computation and outputs as tokura_zgeev_batched_gpu, but it allocates
+ * nothing and takes no workspace: it has no counterpart in the reference.
+ * It is for callers that cannot allocate device memory when they need the
+ * eigenvalues — e.g. code running during a global-mode stream capture, where
+ * cudaMalloc is refused, or plugins whose host application owns all device
+ * memory. The staging area is a 32 MiB static device array in the library
+ * (held by every GPU that loads it until exit), so 16*n*n*batch_count must be
+ * <= tokura_zgeev_noalloc_max_bytes(): at most 512 matrices of order 64,
+ * 2048 of order 32. The first call on a device looks up that array's device
+ * address, so make it before any stream capture starts. All calls share the
+ * array: calls that overlap on the GPU race and must be ordered by the
+ * caller (e.g. one stream). A is not modified.
+ * Returns the codes of tokura_zgeev_batched_gpu (no -5: there is no work),
+ * -8 if the batch exceeds the static array, 1 if the address lookup or the
+ * launch fails. */
+TOKURA_API int tokura_zgeev_batched_gpu_noalloc(tokurablas_t* handle, int n, int batch_count, cuDoubleComplex* A,
+                                                cuDoubleComplex* eigenvalues, char* flag, cudaStream_t cudastream);
+
+/* Size in bytes of the static array behind tokura_zgeev_batched_gpu_noalloc (32 MiB). */
+TOKURA_API size_t tokura_zgeev_noalloc_max_bytes(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -39,6 +39,12 @@ _SIGNATURES = {
     ),
     "tokura_probe_fp64_peak": (
         ctypes.c_int, [ctypes.POINTER(ctypes.c_double), ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]),
+    "tokura_zgeev_batched_gpu_noalloc": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+         ctypes.c_void_p],
+    ),
+    "tokura_zgeev_noalloc_max_bytes": (ctypes.c_size_t, []),
 }
 
 
@@ -142,6 +148,17 @@ def tokura_zgeev_batched_gpu(handle, n: int, batch_count: int, A: int, eigenvalu
     """Raw entry point: device addresses as integers, returns the C status."""
     return int(lib().tokura_zgeev_batched_gpu(_ptr(handle), int(n), int(batch_count), A, eigenvalues, work, flag,
                                               cudastream))
+
+
+def tokura_zgeev_batched_gpu_noalloc(handle, n: int, batch_count: int, A: int, eigenvalues: int, flag: int,
+                                     cudastream: int = 0) -> int:
+    """Workspace-free entry point (static device staging array; see include/tokura_blas_ext.h)."""
+    return int(lib().tokura_zgeev_batched_gpu_noalloc(_ptr(handle), int(n), int(batch_count), A, eigenvalues, flag,
+                                                      cudastream))
+
+
+def noalloc_max_bytes() -> int:
+    return int(lib().tokura_zgeev_noalloc_max_bytes())
 
 
 _DEFAULT_HANDLE = None

@@ -28,6 +28,7 @@ NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibilit
 SOURCES = [
     "zgeev_plain.cu",
     "peak_probe.cu",
+    "zgeev_noalloc.cu",
     "tokura_capi.cpp",
     "compat_cxx.cpp",
 ]
