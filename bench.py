@@ -194,6 +194,127 @@ def run_reference(args):
 
 # ----------------------------------------------------------------------------- our arm
 
+def time_ms(fn, reps: int, stream) -> float:
+    """Average CUDA-event time of fn() on `stream` over reps calls (after one warm-up call)."""
+    import torch
+
+    fn()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def measure_config1(h, dev, stream, peak, call) -> dict:
+    """10,000 complex Gaussian 32x32 matrices, one plain call (the small-batch configuration)."""
+    import torch
+
+    from tokura_zgeev_batched_gb300 import api, workloads
+
+    n, batch = 32, 10000
+    A = workloads.torch_gaussian(batch, n, seed=SEED + 1, device=str(dev))
+    eig = torch.empty(batch, n, dtype=torch.complex128, device=dev)
+    flag = torch.empty(batch, dtype=torch.int8, device=dev)
+    work = torch.empty(api.tokura_get_zgeeveigenvaluesgetworspacesize(n, batch), dtype=torch.uint8, device=dev)
+    ms = time_ms(lambda: call(n, batch, A, eig, flag, work), 5, stream)
+    rate = batch / (ms * 1e-3)
+    return {"n": n, "batch": batch, "ms": ms, "matrices_per_s": rate, "fp64_frac": flops_per_matrix(n) * rate / peak,
+            "lanes_per_matrix": h.plain_config(n, batch)[0], "flagged": int((flag != 0).sum().item())}
+
+
+def measure_ragged(h, dev, stream, peak, batch: int = 200000) -> dict:
+    """Ragged configuration: 200,000 complex Gaussian matrices, n ~ U{1..64} (seeded).
+
+    The same matrices are solved (a) by one ragged call (persistent launch,
+    replayed from a CUDA graph) and (b) by per-size plain launches on the same
+    data grouped by n. Matrices sit in one buffer grouped by n; the ragged call
+    sees them in the random order of their sizes through its offsets array.
+    """
+    import numpy as np
+    import torch
+
+    from tokura_zgeev_batched_gb300 import api, workloads
+
+    ns = workloads.ragged_sizes(batch, 1, 64, seed=SEED + 3)
+    order = np.argsort(ns, kind="stable")
+    sizes_sorted = ns[order].astype(np.int64) ** 2
+    start_sorted = np.concatenate([[0], np.cumsum(sizes_sorted)[:-1]])
+    offsets = np.empty(batch, np.int64)
+    offsets[order] = start_sorted
+    total = int(sizes_sorted.sum())
+    g = torch.Generator(device=dev)
+    g.manual_seed(SEED + 4)
+    A = torch.complex(torch.randn(total, generator=g, device=dev, dtype=torch.float64),
+                      torch.randn(total, generator=g, device=dev, dtype=torch.float64))
+    n_d = torch.from_numpy(ns).to(dev)
+    o_d = torch.from_numpy(offsets).to(dev)
+    total_eig = int(ns.sum())
+    eig = torch.empty(total_eig, dtype=torch.complex128, device=dev)
+    flag = torch.empty(batch, dtype=torch.int8, device=dev)
+    work = torch.empty(api.tokura_get_zgeev_ragged_workspacesize(batch, total), dtype=torch.uint8, device=dev)
+    s = stream.cuda_stream
+
+    def ragged_call():
+        st = api.tokura_zgeev_ragged_gpu(h, batch, n_d.data_ptr(), o_d.data_ptr(), None, total, A.data_ptr(),
+                                         eig.data_ptr(), work.data_ptr(), flag.data_ptr(), s)
+        assert st == 0
+
+    ms_ragged = time_ms(ragged_call, 3, stream)
+    flagged = int((flag != 0).sum().item())
+    # CUDA graph of the ragged call (planning kernels + persistent solver).
+    graph_ms = None
+    try:
+        gs = torch.cuda.Stream(dev)
+        gs.wait_stream(stream)
+        cg = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(cg, stream=gs):
+            st = api.tokura_zgeev_ragged_gpu(h, batch, n_d.data_ptr(), o_d.data_ptr(), None, total, A.data_ptr(),
+                                             eig.data_ptr(), work.data_ptr(), flag.data_ptr(),
+                                             torch.cuda.current_stream().cuda_stream)
+            assert st == 0
+        graph_ms = time_ms(cg.replay, 3, stream)
+        del cg
+    except RuntimeError as exc:  # pragma: no cover - reported, not fatal
+        graph_ms = f"capture failed: {exc}"
+    # Per-size plain launches on the same data (grouped by n).
+    counts = np.bincount(ns, minlength=65)
+    starts = {}
+    pos = 0
+    epos = 0
+    for k in range(1, 65):
+        starts[k] = (pos, epos)
+        pos += int(counts[k]) * k * k
+        epos += int(counts[k]) * k
+    eig2 = torch.empty(total_eig, dtype=torch.complex128, device=dev)
+    flag2 = torch.empty(batch, dtype=torch.int8, device=dev)
+    wmax = max(api.tokura_get_zgeeveigenvaluesgetworspacesize(k, int(counts[k])) for k in range(1, 65) if counts[k])
+    work2 = torch.empty(wmax, dtype=torch.uint8, device=dev)
+    fbase = np.concatenate([[0], np.cumsum(counts[1:])])
+
+    def per_size_calls():
+        for k in range(1, 65):
+            c = int(counts[k])
+            if c == 0:
+                continue
+            p0, e0 = starts[k]
+            st = api.tokura_zgeev_batched_gpu(h, k, c, A.data_ptr() + 16 * p0, eig2.data_ptr() + 16 * e0,
+                                              work2.data_ptr(), flag2.data_ptr() + int(fbase[k - 1]), s)
+            assert st == 0
+
+    ms_plain = time_ms(per_size_calls, 2, stream)
+    work_flops = float(np.sum(40.0 * ns.astype(np.float64) ** 3))
+    best = graph_ms if isinstance(graph_ms, float) else ms_ragged
+    return {"batch": batch, "total_elements": total, "ms_ragged": ms_ragged, "ms_ragged_graph": graph_ms,
+            "ms_per_size_plain": ms_plain, "matrices_per_s_ragged": batch / (best * 1e-3),
+            "matrices_per_s_per_size_plain": batch / (ms_plain * 1e-3), "speedup_vs_per_size": ms_plain / best,
+            "fp64_frac": work_flops / (best * 1e-3) / peak, "lanes_per_matrix": None, "flagged": flagged,
+            "plain_launches": int(np.count_nonzero(counts))}
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -364,6 +485,13 @@ def run_ours(args):
         sweep[str(N)] = {"batch": BATCH, "matrices_per_s": value / ws, "fp64_frac": achieved / peak,
                          "flagged": flagged}
 
+    ragged = None
+    if not args.no_ragged:
+        ragged = measure_ragged(h, dev, stream, peak)
+    config1 = None
+    if not args.no_sweep:
+        config1 = measure_config1(h, dev, stream, peak, call)
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(N)
@@ -379,6 +507,7 @@ def run_ours(args):
                        "lanes_per_matrix": h.plain_config(N, BATCH)[0]},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
             "gpu_launches": args.steps, "flagged": flagged, "parity_spot_check": parity, "sweep": sweep,
+            "config1_n32_10000": config1, "ragged": ragged,
         }
         print(json.dumps(out), flush=True)
     if dist is not None:
@@ -395,6 +524,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-check", action="store_true")
+    ap.add_argument("--no-ragged", action="store_true")
     ap.add_argument("--n", type=int, default=N, help="matrix order of the timed workload (profiling cases)")
     ap.add_argument("--batch", type=int, default=0, help="matrices per GPU (default: 4 GiB of input)")
     args = ap.parse_args()

@@ -38,6 +38,34 @@ TOKURA_API int tokuraGetPlainConfig(const tokurablas_t* handle, int n, int batch
 TOKURA_API int tokura_probe_fp64_peak(double* flops_per_second, double* scratch, int scratch_doubles,
                                       cudaStream_t stream);
 
+/* Ragged batch: matrix j has its own order n[j] (1..64) and starts at element
+ * offsets[j] of A (column-major, 16*n[j]^2 bytes), A holding total_elements
+ * complex entries. Its eigenvalues go to eigenvalues[eig_offsets[j] + i]; if
+ * eig_offsets is NULL they follow one another (exclusive prefix sum of n).
+ * One persistent launch pulls size-bucketed tiles (largest n first) from a
+ * device work queue; planning runs on the device, so the call is
+ * asynchronous and can be captured in a CUDA graph. flag[j] as for the plain
+ * call, plus 3 when n[j] or offsets[j] is invalid (order outside 1..64, or
+ * the matrix does not lie inside A) or the matrices' sizes sum to more than
+ * total_elements. n, offsets, eig_offsets: device arrays of batch_count.
+ * work: tokura_get_zgeev_ragged_workspacesize(batch_count, total_elements)
+ * bytes. The reference has no counterpart (it takes one n per call).
+ * Returns 0; -1 NULL handle, -2 n NULL, -3 A NULL, -4 eigenvalues NULL,
+ * -5 work NULL, -6 batch_count <= 0, -7 flag NULL, -8 offsets NULL,
+ * -9 total_elements <= 0; 1 launch failure. */
+TOKURA_API int tokura_zgeev_ragged_gpu(tokurablas_t* handle, int batch_count, const int* n, const long long* offsets,
+                                       const long long* eig_offsets, long long total_elements,
+                                       const cuDoubleComplex* A, cuDoubleComplex* eigenvalues, void* work, char* flag,
+                                       cudaStream_t stream);
+
+/* Workspace bytes of tokura_zgeev_ragged_gpu: 16*total_elements staging plus
+ * the work queue and bookkeeping; (size_t)-2 if batch_count <= 0,
+ * (size_t)-3 if total_elements <= 0. */
+TOKURA_API size_t tokura_get_zgeev_ragged_workspacesize(int batch_count, long long total_elements);
+
+/* Lanes per matrix of the ragged solver (1, 2, 4; 0 = choose from batch_count). */
+TOKURA_API int tokuraSetRaggedLanes(tokurablas_t* handle, int lanes_per_matrix);
+
 /* Same computation and outputs as tokura_zgeev_batched_gpu, but it allocates
  * nothing and takes no workspace: it has no counterpart in the reference.
  * It is for callers that cannot allocate device memory when they need the

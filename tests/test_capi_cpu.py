@@ -118,3 +118,27 @@ def test_c_caller_compiles_against_header(tmp_path):
     r = subprocess.run(["gcc", "-std=c99", "-c", str(src), "-I", os.path.join(ROOT, "include"), "-I",
                         "/usr/local/cuda/include", "-o", str(tmp_path / "c_caller.o")], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_ragged_workspace_size(lib):
+    ws = api.tokura_get_zgeev_ragged_workspacesize
+    size_max = 2 ** 64 - 1
+    assert ws(0, 10) == size_max - 1 and ws(5, 0) == size_max - 2
+    b, t = 200000, 200000 * 1400
+    need = ws(b, t)
+    assert need >= 16 * t + 12 * b and need % 256 == 0 and need < 16 * t + 12 * b + 64 * 1024
+
+
+def test_ragged_argument_validation(lib):
+    fake = ctypes.c_void_p(0x1000)
+    p = 0x2000
+    f = api.tokura_zgeev_ragged_gpu
+    assert f(None, 4, p, p, None, 100, p, p, p, p) == -1
+    assert f(fake, 4, None, p, None, 100, p, p, p, p) == -2
+    assert f(fake, 4, p, p, None, 100, None, p, p, p) == -3
+    assert f(fake, 4, p, p, None, 100, p, None, p, p) == -4
+    assert f(fake, 4, p, p, None, 100, p, p, None, p) == -5
+    assert f(fake, 0, p, p, None, 100, p, p, p, p) == -6
+    assert f(fake, 4, p, p, None, 100, p, p, p, None) == -7
+    assert f(fake, 4, p, None, None, 100, p, p, p, p) == -8
+    assert f(fake, 4, p, p, None, 0, p, p, p, p) == -9

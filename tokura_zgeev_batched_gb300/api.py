@@ -45,6 +45,13 @@ _SIGNATURES = {
          ctypes.c_void_p],
     ),
     "tokura_zgeev_noalloc_max_bytes": (ctypes.c_size_t, []),
+    "tokura_zgeev_ragged_gpu": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong,
+         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
+    ),
+    "tokura_get_zgeev_ragged_workspacesize": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_longlong]),
+    "tokuraSetRaggedLanes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
 }
 
 
@@ -97,6 +104,9 @@ class Handle:
         if st != 0:
             raise ValueError(f"tokuraGetPlainConfig returned {st}")
         return lanes.value, threads.value
+
+    def set_ragged_lanes(self, lanes: int) -> int:
+        return int(lib().tokuraSetRaggedLanes(self.ptr, int(lanes)))
 
     def close(self):
         if self.ptr is not None and self.ptr.value:
@@ -219,3 +229,60 @@ def probe_fp64_peak(device=None) -> float:
     if st != 0:
         raise RuntimeError(f"tokura_probe_fp64_peak returned {st}")
     return out.value
+
+
+def tokura_get_zgeev_ragged_workspacesize(batch_count: int, total_elements: int) -> int:
+    return int(lib().tokura_get_zgeev_ragged_workspacesize(int(batch_count), int(total_elements)))
+
+
+def tokura_zgeev_ragged_gpu(handle, batch_count: int, n: int, offsets: int, eig_offsets: int | None,
+                            total_elements: int, A: int, eigenvalues: int, work: int, flag: int,
+                            stream: int = 0) -> int:
+    """Raw ragged entry point (device addresses as integers)."""
+    return int(lib().tokura_zgeev_ragged_gpu(_ptr(handle), int(batch_count), n, offsets, eig_offsets,
+                                             int(total_elements), A, eigenvalues, work, flag, stream))
+
+
+def zgeev_ragged(A_packed, n, offsets=None, eig_offsets=None, handle: Handle | None = None, work=None,
+                 stream=None):
+    """Eigenvalues of a ragged batch on the GPU.
+
+    ``A_packed``: 1-D complex128 CUDA tensor with the matrices one after another
+    (column-major each); ``n``: int32 CUDA tensor of orders; ``offsets``: int64
+    element offsets (default: packed, exclusive prefix sum of n^2). Returns
+    ``(eigenvalues, flag)`` with eigenvalues packed by the prefix sum of n
+    unless ``eig_offsets`` is given (then the output holds ``max(eig_offsets + n)`` entries).
+    """
+    import torch
+
+    if not A_packed.is_cuda or A_packed.dtype != torch.complex128 or A_packed.dim() != 1:
+        raise TypeError("A_packed must be a 1-D complex128 CUDA tensor")
+    dev = A_packed.device
+    n = n.to(device=dev, dtype=torch.int32).contiguous()
+    batch = n.numel()
+    n64 = n.to(torch.int64)
+    if offsets is None:
+        offsets = torch.cumsum(n64 * n64, 0) - n64 * n64
+    offsets = offsets.to(device=dev, dtype=torch.int64).contiguous()
+    if eig_offsets is None:
+        total_eig = int(n64.sum().item()) if batch else 0
+        eptr = None
+    else:
+        eig_offsets = eig_offsets.to(device=dev, dtype=torch.int64).contiguous()
+        total_eig = int((eig_offsets + n64).max().item()) if batch else 0
+        eptr = eig_offsets.data_ptr()
+    eig = torch.empty(max(total_eig, 1), dtype=torch.complex128, device=dev)
+    flag = torch.empty(batch, dtype=torch.int8, device=dev)
+    if batch == 0:
+        return eig[:0], flag
+    total = A_packed.numel()
+    need = tokura_get_zgeev_ragged_workspacesize(batch, total)
+    if work is None or work.numel() * work.element_size() < need:
+        work = torch.empty(need, dtype=torch.uint8, device=dev)
+    s = stream if stream is not None else torch.cuda.current_stream(dev)
+    h = handle if handle is not None else default_handle()
+    st = tokura_zgeev_ragged_gpu(h, batch, n.data_ptr(), offsets.data_ptr(), eptr, total, A_packed.data_ptr(),
+                                 eig.data_ptr(), work.data_ptr(), flag.data_ptr(), s.cuda_stream)
+    if st != 0:
+        raise RuntimeError(f"tokura_zgeev_ragged_gpu returned {st}")
+    return eig[:total_eig], flag

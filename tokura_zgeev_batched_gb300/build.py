@@ -29,6 +29,7 @@ SOURCES = [
     "zgeev_plain.cu",
     "peak_probe.cu",
     "zgeev_noalloc.cu",
+    "zgeev_ragged.cu",
     "tokura_capi.cpp",
     "compat_cxx.cpp",
 ]

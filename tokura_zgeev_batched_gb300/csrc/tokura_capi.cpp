@@ -85,3 +85,37 @@ extern "C" int tokuraGetPlainConfig(const tokurablas_t* handle, int n, int batch
   *threads_per_block = c.threads;
   return 0;
 }
+
+extern "C" size_t tokura_get_zgeev_ragged_workspacesize(int batch_count, long long total_elements) {
+  if (!(batch_count > 0)) return (size_t)-2;
+  if (!(total_elements > 0)) return (size_t)-3;
+  return tzg::ragged_workspace_bytes(batch_count, total_elements);
+}
+
+extern "C" int tokura_zgeev_ragged_gpu(tokurablas_t* handle, int batch_count, const int* n, const long long* offsets,
+                                       const long long* eig_offsets, long long total_elements,
+                                       const cuDoubleComplex* A, cuDoubleComplex* eigenvalues, void* work, char* flag,
+                                       cudaStream_t stream) {
+  if (handle == nullptr) return -1;
+  if (n == nullptr) return -2;
+  if (A == nullptr) return -3;
+  if (eigenvalues == nullptr) return -4;
+  if (work == nullptr) return -5;
+  if (!(batch_count > 0)) return -6;
+  if (flag == nullptr) return -7;
+  if (offsets == nullptr) return -8;
+  if (!(total_elements > 0)) return -9;
+  const int lanes = tzg::ragged_lanes_for(handle, batch_count);
+  const cudaError_t err = tzg::launch_ragged(lanes, handle->sm_count, batch_count, n, offsets, eig_offsets,
+                                             total_elements, reinterpret_cast<const double2*>(A),
+                                             reinterpret_cast<double2*>(eigenvalues), work, flag,
+                                             handle->itmax_override, stream);
+  return err == cudaSuccess ? 0 : 1;
+}
+
+extern "C" int tokuraSetRaggedLanes(tokurablas_t* handle, int lanes_per_matrix) {
+  if (handle == nullptr) return -1;
+  if (!(lanes_per_matrix == 0 || lanes_per_matrix == 1 || lanes_per_matrix == 2 || lanes_per_matrix == 4)) return -3;
+  handle->ragged_lanes = lanes_per_matrix;
+  return 0;
+}

@@ -9,6 +9,7 @@ struct tokurablas_t {
   int itmax_override = 0;  // >0 replaces the per-eigenvalue sweep cap 30*max(10,n)
   // Tuned plain-kernel shape per n (index 1..64); lanes == 0 means "heuristic".
   tzg::PlainConfig plain[65] = {};
+  int ragged_lanes = 0;  // lanes per matrix of the ragged solver; 0 = heuristic
 };
 
 namespace tzg {
@@ -34,6 +35,17 @@ inline PlainConfig plain_config_for(const tokurablas_t* h, int n, int batch) {
   }
   if (c.threads == 0) c.threads = 128;
   return c;
+}
+
+inline int lanes_for_batch(const tokurablas_t* h, long long batch) {
+  const long long want_lanes = (long long)h->sm_count * 4 * 2 * 32;
+  if (batch >= want_lanes) return 1;
+  if (batch * 2 >= want_lanes) return 2;
+  return 4;
+}
+
+inline int ragged_lanes_for(const tokurablas_t* h, long long batch) {
+  return h->ragged_lanes > 0 ? h->ragged_lanes : lanes_for_batch(h, batch);
 }
 
 }  // namespace tzg

@@ -13,7 +13,7 @@ namespace tzg {
 
 // Result codes of the per-matrix solve, stored in flag[] (0 = converged,
 // which is the reference's contract, tokura_zhseqr_MWB_kernel.cuh:768-776).
-enum : int { kConverged = 0, kNotConverged = 1, kNonFinite = 2 };
+enum : int { kConverged = 0, kNotConverged = 1, kNonFinite = 2, kInvalidInput = 3 };
 
 // Stage matrix `slot` of a tile from column-major `src` (n*n elements) into
 // the tile-interleaved view, scaling by an exact power of two when the
@@ -48,6 +48,60 @@ __device__ __forceinline__ int stage_and_scale(const double2* __restrict__ src, 
   }
   G.sync();
   return shift;
+}
+
+// Applies P = I - tau v v^H (v[0] = 1, v[i] at x[i*xs]) to NV vectors of
+// length m at p[k][i*es]: a <- a - tau v (v^H a). With kConjV the reflector
+// acts from the right on rows instead: a <- a - tau (a v) v^H, which is the
+// same formula with v conjugated. The NV dot products share the loads of v
+// and run as independent FMA chains; the update loop loads element i+1
+// before storing element i so memory latency overlaps the arithmetic.
+template <int NV, bool kConjV>
+__device__ __forceinline__ void reflect_vectors(double2* const (&p)[NV], const double2* x, int m, int es, int xs,
+                                                double tau) {
+  double2 w[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) w[k] = p[k][0];
+  for (int i = 1; i < m; ++i) {
+    const double2 v = x[i * xs];
+    const double vy = kConjV ? -v.y : v.y;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      const double2 a = p[k][i * es];
+      w[k].x = fma(v.x, a.x, fma(vy, a.y, w[k].x));
+      w[k].y = fma(v.x, a.y, fma(-vy, a.x, w[k].y));
+    }
+  }
+  double2 t[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    t[k] = make_double2(w[k].x * tau, w[k].y * tau);
+    p[k][0] = csub(p[k][0], t[k]);
+  }
+  if (m < 2) return;
+  double2 v = x[xs];
+  double2 a[NV];
+#pragma unroll
+  for (int k = 0; k < NV; ++k) a[k] = p[k][es];
+  for (int i = 1; i < m; ++i) {
+    double2 vn = v, an[NV];
+    if (i + 1 < m) {
+      vn = x[(i + 1) * xs];
+#pragma unroll
+      for (int k = 0; k < NV; ++k) an[k] = p[k][(i + 1) * es];
+    }
+    const double vy = kConjV ? -v.y : v.y;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      // a -= v' t, v' = (v.x, vy)
+      a[k].x = fma(-v.x, t[k].x, fma(vy, t[k].y, a[k].x));
+      a[k].y = fma(-v.x, t[k].y, fma(-vy, t[k].x, a[k].y));
+      p[k][i * es] = a[k];
+    }
+    v = vn;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) a[k] = an[k];
+  }
 }
 
 // Householder reduction to upper Hessenberg form, in place. The reflector for
@@ -93,46 +147,29 @@ __device__ void hessenberg(const MatView& M, const Group<L>& G) {
     for (int i = 1 + G.rank; i < m; i += L) x[i * rs] = cmul(x[i * rs], cg);
     G.sync();
     if (G.rank == 0) x[0] = alpha;
-    // Left update: H[r+1:, c] -= tau v (v^H H[r+1:, c]) for c = r+1 .. n-1.
-    for (int c = r + 1 + G.rank; c < n; c += L) {
-      double2* col = M.at(r + 1, c);
-      double2 w = col[0];
-      for (int i = 1; i < m; ++i) {
-        const double2 v = x[i * rs];
-        const double2 a = col[i * rs];
-        w.x = fma(v.x, a.x, fma(v.y, a.y, w.x));
-        w.y = fma(v.x, a.y, fma(-v.y, a.x, w.y));
+    // Left update: H[r+1:, c] -= tau v (v^H H[r+1:, c]) for c = r+1 .. n-1, two columns at a time.
+    {
+      int c = r + 1 + G.rank;
+      for (; c + L < n; c += 2 * L) {
+        double2* p[2] = {M.at(r + 1, c), M.at(r + 1, c + L)};
+        reflect_vectors<2, false>(p, x, m, rs, rs, tau);
       }
-      const double2 t = make_double2(w.x * tau, w.y * tau);
-      col[0] = csub(col[0], t);
-      for (int i = 1; i < m; ++i) {
-        const double2 v = x[i * rs];
-        double2 a = col[i * rs];
-        a.x = fma(-v.x, t.x, fma(v.y, t.y, a.x));
-        a.y = fma(-v.x, t.y, fma(-v.y, t.x, a.y));
-        col[i * rs] = a;
+      if (c < n) {
+        double2* p[1] = {M.at(r + 1, c)};
+        reflect_vectors<1, false>(p, x, m, rs, rs, tau);
       }
     }
     G.sync();
-    // Right update: H[q, r+1:] -= tau (H[q, r+1:] v) v^H for every row q.
-    for (int q = G.rank; q < n; q += L) {
-      double2* row = M.at(q, r + 1);
-      double2 y = row[0];
-      for (int i = 1; i < m; ++i) {
-        const double2 v = x[i * rs];
-        const double2 a = row[i * cs];
-        y.x = fma(a.x, v.x, fma(-a.y, v.y, y.x));
-        y.y = fma(a.x, v.y, fma(a.y, v.x, y.y));
+    // Right update: H[q, r+1:] -= tau (H[q, r+1:] v) v^H for every row q, two rows at a time.
+    {
+      int q = G.rank;
+      for (; q + L < n; q += 2 * L) {
+        double2* p[2] = {M.at(q, r + 1), M.at(q + L, r + 1)};
+        reflect_vectors<2, true>(p, x, m, cs, rs, tau);
       }
-      const double2 t = make_double2(y.x * tau, y.y * tau);
-      row[0] = csub(row[0], t);
-      for (int i = 1; i < m; ++i) {
-        const double2 v = x[i * rs];
-        double2 a = row[i * cs];
-        // a -= t conj(v)
-        a.x = fma(-t.x, v.x, fma(-t.y, v.y, a.x));
-        a.y = fma(-t.y, v.x, fma(t.x, v.y, a.y));
-        row[i * cs] = a;
+      if (q < n) {
+        double2* p[1] = {M.at(q, r + 1)};
+        reflect_vectors<1, true>(p, x, m, cs, rs, tau);
       }
     }
     G.sync();
@@ -222,11 +259,22 @@ __device__ int qr_eigenvalues(const MatView& M, const Group<L>& G, double2* __re
         const Rot g = make_rot(x, y, rr);
         G.sync();  // all lanes have read the bulge before it is overwritten
         if (j > lo && G.rank == 0) *M.at(j, j - 1) = rr;
-        // Left: rows (j, j+1), columns j .. i.
+        // Left: rows (j, j+1), columns j .. i (next pair loaded before the current one is stored).
         {
-          double2* pc = M.at(j, j + G.rank);
-          for (int c = j + G.rank; c <= i; c += L, pc += L * cs) {
+          const int c0 = j + G.rank;
+          if (c0 <= i) {
+            double2* pc = M.at(j, c0);
             double2 a = pc[0], b = pc[rs];
+            for (int c = c0 + L; c <= i; c += L) {
+              double2* pn = pc + L * cs;
+              const double2 an = pn[0], bn = pn[rs];
+              rot_left(g, a, b);
+              pc[0] = a;
+              pc[rs] = b;
+              a = an;
+              b = bn;
+              pc = pn;
+            }
             rot_left(g, a, b);
             pc[0] = a;
             pc[rs] = b;
@@ -237,9 +285,20 @@ __device__ int qr_eigenvalues(const MatView& M, const Group<L>& G, double2* __re
         // new bulge (its column-j entry is zero before the rotation).
         {
           const int qend = min(j + 1, i);
-          double2* pr = M.at(lo + G.rank, j);
-          for (int q = lo + G.rank; q <= qend; q += L, pr += L * rs) {
+          const int q0 = lo + G.rank;
+          if (q0 <= qend) {
+            double2* pr = M.at(q0, j);
             double2 a = pr[0], b = pr[cs];
+            for (int q = q0 + L; q <= qend; q += L) {
+              double2* pn = pr + L * rs;
+              const double2 an = pn[0], bn = pn[cs];
+              rot_right(g, a, b);
+              pr[0] = a;
+              pr[cs] = b;
+              a = an;
+              b = bn;
+              pr = pn;
+            }
             rot_right(g, a, b);
             pr[0] = a;
             pr[cs] = b;
@@ -274,6 +333,22 @@ __device__ int qr_eigenvalues(const MatView& M, const Group<L>& G, double2* __re
     }
   }
   return status;
+}
+
+// Full solve of one matrix by its lane group: stage (with exact pre-scaling),
+// Hessenberg reduction, QR, eigenvalue write-out. Returns the flag value.
+template <int L>
+__device__ __forceinline__ int solve_matrix(const double2* __restrict__ src, const MatView& M, const Group<L>& G,
+                                            double2* __restrict__ ev, int itmax) {
+  bool nonfinite, zero;
+  const int shift = stage_and_scale<L>(src, M, G, nonfinite, zero);
+  if (nonfinite || zero) {
+    const double v = nonfinite ? __longlong_as_double(0x7ff8000000000000LL) : 0.0;
+    for (int i = G.rank; i < M.n; i += L) ev[i] = make_double2(v, v);
+    return nonfinite ? kNonFinite : kConverged;
+  }
+  hessenberg<L>(M, G);
+  return qr_eigenvalues<L>(M, G, ev, shift, itmax);
 }
 
 }  // namespace tzg

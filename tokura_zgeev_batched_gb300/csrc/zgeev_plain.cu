@@ -28,17 +28,7 @@ __global__ void __launch_bounds__(256) zgeev_plain_kernel(int n, int batch, cons
   const long long j = g0 + slot;
   MatView M{work + g0 * nn + slot, n, tw};
 
-  bool nonfinite, zero;
-  const int shift = stage_and_scale<L>(A + j * nn, M, G, nonfinite, zero);
-  double2* ev = eig + j * n;
-  if (nonfinite || zero) {
-    const double v = nonfinite ? __longlong_as_double(0x7ff8000000000000LL) : 0.0;
-    for (int i = G.rank; i < n; i += L) ev[i] = make_double2(v, v);
-    if (G.rank == 0) flag[j] = (char)(nonfinite ? kNonFinite : kConverged);
-    return;
-  }
-  hessenberg<L>(M, G);
-  const int status = qr_eigenvalues<L>(M, G, ev, shift, itmax);
+  const int status = solve_matrix<L>(A + j * nn, M, G, eig + j * n, itmax);
   if (G.rank == 0) flag[j] = (char)status;
 }
 
