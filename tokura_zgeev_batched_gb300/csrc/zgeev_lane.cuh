@@ -214,14 +214,19 @@ __device__ int qr_eigenvalues(const MatView& M, const Group<L>& G, double2* __re
   const double smlnum = kSafeMin * ((double)n / kUlp);
   const double unscale = (shift != 0) ? pow2(shift) : 1.0;
   int status = kConverged;
-  int i = n - 1;
-  int kdefl = 0;
-  while (i >= 0) {
-    int lo = 0;
-    bool done = false;
-    for (int its = 0; its <= itmax; ++its) {
-      // Locate the lowest negligible subdiagonal in (lo, i]; lanes scan
-      // interleaved k's from the bottom and the group keeps the largest hit.
+  int i = n - 1;   // last unconverged row
+  int lo = 0;      // top of the active block [lo, i]
+  int its = 0;     // sweeps since the last deflation (LAPACK's per-eigenvalue cap)
+  int kdefl = 0;   // sweeps since the last deflation, for ad hoc shifts
+  // One loop iteration = (deflations, then) one sweep. Lanes of a warp hold
+  // different matrices; keeping them in lockstep per sweep rather than per
+  // eigenvalue means a lane whose eigenvalue converged early goes straight
+  // on to its next sweep instead of idling until every lane has converged.
+  while (true) {
+    // Deflation: peel converged entries off the bottom (usually 0 or 1 per sweep).
+    for (;;) {
+      // Lowest negligible subdiagonal in (lo, i]; lanes scan interleaved k's
+      // from the bottom and the group keeps the largest hit.
       int hit = lo;
       for (int k = i - G.rank; k > lo; k -= L) {
         if (negligible_subdiag(M, k, lo, i, smlnum)) {
@@ -230,11 +235,25 @@ __device__ int qr_eigenvalues(const MatView& M, const Group<L>& G, double2* __re
         }
       }
       lo = G.imax(hit);
-      if (lo >= i) {
-        done = true;
-        break;
+      if (lo < i) break;
+      if (G.rank == 0) {
+        const double2 d = *M.at(i, i);
+        eig_out[i] = make_double2(d.x * unscale, d.y * unscale);
       }
-      ++kdefl;
+      i -= 1;
+      lo = 0;
+      its = 0;
+      kdefl = 0;
+      if (i < 0) break;
+    }
+    if (i < 0) break;
+    if (its > itmax) {
+      status = kNotConverged;
+      break;
+    }
+    ++its;
+    ++kdefl;
+    {
       // Shift selection.
       double2 sigma;
       if (kdefl % (2 * kExceptionalPeriod) == 0) {
@@ -314,16 +333,6 @@ __device__ int qr_eigenvalues(const MatView& M, const Group<L>& G, double2* __re
         G.sync();
       }
     }
-    if (!done) {
-      status = kNotConverged;
-      break;
-    }
-    if (G.rank == 0) {
-      const double2 d = *M.at(i, i);
-      eig_out[i] = make_double2(d.x * unscale, d.y * unscale);
-    }
-    kdefl = 0;
-    i = lo - 1;
   }
   if (status != kConverged && G.rank == 0) {
     // Unconverged positions 0..i carry their current diagonal entries.
