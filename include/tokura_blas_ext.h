@@ -32,6 +32,29 @@ TOKURA_API int tokuraSetPlainConfig(tokurablas_t* handle, int n, int lanes_per_m
 TOKURA_API int tokuraGetPlainConfig(const tokurablas_t* handle, int n, int batch_count, int* lanes_per_matrix,
                                     int* threads_per_block);
 
+/* Autotuner (replaces the reference's build-time tuner,
+ * src/TOKURA_ZHSEQR_BATCHED_GEHRD_TUNING_main.cu:89-227, and its generated
+ * tables). For each order n in [n_min, n_max], times every plain-kernel shape
+ * (lanes per matrix 1/2/4 x threads per block 64/128/256) on batch_count
+ * seeded synthetic complex Gaussian matrices and stores the fastest in the
+ * handle. Allocates its own scratch (cudaMalloc), synchronizes `stream`.
+ * Returns 0; -1 NULL handle, -2 bad range, -6 batch_count <= 0,
+ * 2 allocation failure, 1 CUDA failure. */
+TOKURA_API int tokuraAutotune(tokurablas_t* handle, int n_min, int n_max, int batch_count, cudaStream_t stream);
+
+/* Same for the ragged solver (lanes per matrix) on batch_count matrices with
+ * orders uniform in [n_min, n_max]. */
+TOKURA_API int tokuraAutotuneRagged(tokurablas_t* handle, int batch_count, int n_min, int n_max,
+                                    cudaStream_t stream);
+
+/* Writes / reads the handle's tuned shapes as a text file keyed by device name
+ * and SM count. Load returns 0; 1 cannot open, 2 malformed, 3 the file was
+ * tuned on another device (the handle is left unchanged unless 0).
+ * tokuraCreate applies the file named by the environment variable
+ * TOKURA_ZGEEV_TUNING_FILE when it matches the device. */
+TOKURA_API int tokuraSaveTuning(const tokurablas_t* handle, const char* path);
+TOKURA_API int tokuraLoadTuning(tokurablas_t* handle, const char* path);
+
 /* Measures the device's FP64 FMA throughput (FLOP/s, 2 per FMA) with a
  * saturating FMA loop; synchronizes `stream`. scratch: >= 512*SMs doubles.
  * Returns 0, -1 NULL pointer, -2 scratch too small, 1 CUDA failure. */

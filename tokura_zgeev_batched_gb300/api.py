@@ -52,6 +52,11 @@ _SIGNATURES = {
     ),
     "tokura_get_zgeev_ragged_workspacesize": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_longlong]),
     "tokuraSetRaggedLanes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "tokuraAutotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
+    "tokuraAutotuneRagged": (ctypes.c_int,
+                             [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
+    "tokuraSaveTuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
+    "tokuraLoadTuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
 }
 
 
@@ -104,6 +109,19 @@ class Handle:
         if st != 0:
             raise ValueError(f"tokuraGetPlainConfig returned {st}")
         return lanes.value, threads.value
+
+    def autotune(self, n_min: int, n_max: int, batch_count: int, stream: int = 0) -> int:
+        """Times all plain-kernel shapes for orders n_min..n_max and keeps the fastest (synchronizes)."""
+        return int(lib().tokuraAutotune(self.ptr, int(n_min), int(n_max), int(batch_count), stream))
+
+    def autotune_ragged(self, batch_count: int, n_min: int = 1, n_max: int = 64, stream: int = 0) -> int:
+        return int(lib().tokuraAutotuneRagged(self.ptr, int(batch_count), int(n_min), int(n_max), stream))
+
+    def save_tuning(self, path: str) -> int:
+        return int(lib().tokuraSaveTuning(self.ptr, os.fsencode(path)))
+
+    def load_tuning(self, path: str) -> int:
+        return int(lib().tokuraLoadTuning(self.ptr, os.fsencode(path)))
 
     def set_ragged_lanes(self, lanes: int) -> int:
         return int(lib().tokuraSetRaggedLanes(self.ptr, int(lanes)))

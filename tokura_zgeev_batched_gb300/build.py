@@ -30,6 +30,7 @@ SOURCES = [
     "peak_probe.cu",
     "zgeev_noalloc.cu",
     "zgeev_ragged.cu",
+    "tokura_tuner.cu",
     "tokura_capi.cpp",
     "compat_cxx.cpp",
 ]

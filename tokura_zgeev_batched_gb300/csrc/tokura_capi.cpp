@@ -7,6 +7,7 @@
 // Unlike the reference, the handle is not written by calls (the reference
 // stores every call's arguments in it, tokura_zgeev_batched.cu:224-235), and
 // the NULL-handle check happens before any dereference.
+#include <cstdlib>
 #include <new>
 
 #include "../../include/tokura_blas_ext.h"
@@ -25,6 +26,8 @@ extern "C" int tokuraCreate(tokurablas_t** handle) {
     return 1;
   }
   tzg::init_default_tuning(h);
+  // A tuning file written by tokuraSaveTuning for this device is applied if named in the environment.
+  if (const char* path = std::getenv("TOKURA_ZGEEV_TUNING_FILE")) tokuraLoadTuning(h, path);
   *handle = h;
   return 0;
 }
