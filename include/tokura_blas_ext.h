@@ -86,6 +86,36 @@ TOKURA_API int tokura_zgeev_ragged_gpu(tokurablas_t* handle, int batch_count, co
  * (size_t)-3 if total_elements <= 0. */
 TOKURA_API size_t tokura_get_zgeev_ragged_workspacesize(int batch_count, long long total_elements);
 
+/* Differentiable mode (no counterpart in the reference). Given A (as passed to
+ * the forward, column-major), the forward's eigenvalues and the gradients of
+ * a real loss with respect to them (torch's convention for complex tensors:
+ * dL/dRe + i dL/dIm), returns grad_A in A's layout:
+ *     grad_A = Q X^{-H} diag(grad_eigenvalues) X^H Q^H,
+ * with A = Q T Q^H recomputed (Schur form; the forward's eigenvalues serve as
+ * shifts and are matched to the diagonal of T) and X the right eigenvectors of
+ * T. Only A and the eigenvalues need to be kept from the forward.
+ * flag[j]: 0 ok, 1 QR cap hit (grad_A NaN), 2 non-finite A (grad_A NaN),
+ * 4 two eigenvalues coincide to working precision (derivative undefined;
+ * denominators clamped). work: tokura_get_zgeev_backward_workspacesize bytes
+ * (48*n*n*batch + 16*n*batch). Returns 0; -1 NULL handle, -2 bad n, -3 A NULL,
+ * -4 eigenvalues or grad_eigenvalues NULL, -5 work NULL, -6 batch_count <= 0,
+ * -7 flag NULL, -8 grad_A NULL; 1 launch failure. */
+TOKURA_API int tokura_zgeev_backward_gpu(tokurablas_t* handle, int n, int batch_count, const cuDoubleComplex* A,
+                                         const cuDoubleComplex* eigenvalues, const cuDoubleComplex* grad_eigenvalues,
+                                         cuDoubleComplex* grad_A, void* work, char* flag, cudaStream_t stream);
+TOKURA_API size_t tokura_get_zgeev_backward_workspacesize(int n, int batch_count);
+
+/* Ragged backward: layouts as tokura_zgeev_ragged_gpu (grad_A at offsets[j],
+ * eigenvalues and grad_eigenvalues at eig_offsets[j] or packed); flags as the
+ * plain backward plus 3 for invalid entries. -10: grad_A NULL. */
+TOKURA_API int tokura_zgeev_ragged_backward_gpu(tokurablas_t* handle, int batch_count, const int* n,
+                                                const long long* offsets, const long long* eig_offsets,
+                                                long long total_elements, const cuDoubleComplex* A,
+                                                const cuDoubleComplex* eigenvalues,
+                                                const cuDoubleComplex* grad_eigenvalues, cuDoubleComplex* grad_A,
+                                                void* work, char* flag, cudaStream_t stream);
+TOKURA_API size_t tokura_get_zgeev_ragged_backward_workspacesize(int batch_count, long long total_elements);
+
 /* Lanes per matrix of the ragged solver (1, 2, 4; 0 = choose from batch_count). */
 TOKURA_API int tokuraSetRaggedLanes(tokurablas_t* handle, int lanes_per_matrix);
 

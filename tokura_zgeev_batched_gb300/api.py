@@ -56,6 +56,17 @@ _SIGNATURES = {
     "tokuraAutotuneRagged": (ctypes.c_int,
                              [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
     "tokuraSaveTuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
+    "tokura_zgeev_backward_gpu": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 7,
+    ),
+    "tokura_get_zgeev_backward_workspacesize": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int]),
+    "tokura_zgeev_ragged_backward_gpu": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_longlong]
+        + [ctypes.c_void_p] * 7,
+    ),
+    "tokura_get_zgeev_ragged_backward_workspacesize": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_longlong]),
     "tokuraLoadTuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
 }
 
@@ -262,7 +273,7 @@ def tokura_zgeev_ragged_gpu(handle, batch_count: int, n: int, offsets: int, eig_
 
 
 def zgeev_ragged(A_packed, n, offsets=None, eig_offsets=None, handle: Handle | None = None, work=None,
-                 stream=None):
+                 stream=None, total_eigenvalues: int | None = None):
     """Eigenvalues of a ragged batch on the GPU.
 
     ``A_packed``: 1-D complex128 CUDA tensor with the matrices one after another
@@ -270,6 +281,7 @@ def zgeev_ragged(A_packed, n, offsets=None, eig_offsets=None, handle: Handle | N
     element offsets (default: packed, exclusive prefix sum of n^2). Returns
     ``(eigenvalues, flag)`` with eigenvalues packed by the prefix sum of n
     unless ``eig_offsets`` is given (then the output holds ``max(eig_offsets + n)`` entries).
+    Pass ``offsets`` and ``total_eigenvalues`` to avoid host synchronisation.
     """
     import torch
 
@@ -283,7 +295,8 @@ def zgeev_ragged(A_packed, n, offsets=None, eig_offsets=None, handle: Handle | N
         offsets = torch.cumsum(n64 * n64, 0) - n64 * n64
     offsets = offsets.to(device=dev, dtype=torch.int64).contiguous()
     if eig_offsets is None:
-        total_eig = int(n64.sum().item()) if batch else 0
+        # total_eigenvalues avoids a host synchronisation (e.g. under CUDA-graph capture)
+        total_eig = total_eigenvalues if total_eigenvalues is not None else (int(n64.sum().item()) if batch else 0)
         eptr = None
     else:
         eig_offsets = eig_offsets.to(device=dev, dtype=torch.int64).contiguous()
@@ -304,3 +317,50 @@ def zgeev_ragged(A_packed, n, offsets=None, eig_offsets=None, handle: Handle | N
     if st != 0:
         raise RuntimeError(f"tokura_zgeev_ragged_gpu returned {st}")
     return eig[:total_eig], flag
+
+
+def tokura_zgeev_backward_gpu(handle, n: int, batch_count: int, A: int, eigenvalues: int, grad_eigenvalues: int,
+                              grad_A: int, work: int, flag: int, stream: int = 0) -> int:
+    return int(lib().tokura_zgeev_backward_gpu(_ptr(handle), int(n), int(batch_count), A, eigenvalues,
+                                               grad_eigenvalues, grad_A, work, flag, stream))
+
+
+def tokura_get_zgeev_backward_workspacesize(n: int, batch_count: int) -> int:
+    return int(lib().tokura_get_zgeev_backward_workspacesize(int(n), int(batch_count)))
+
+
+def tokura_zgeev_ragged_backward_gpu(handle, batch_count: int, n: int, offsets: int, eig_offsets: int | None,
+                                     total_elements: int, A: int, eigenvalues: int, grad_eigenvalues: int,
+                                     grad_A: int, work: int, flag: int, stream: int = 0) -> int:
+    return int(lib().tokura_zgeev_ragged_backward_gpu(_ptr(handle), int(batch_count), n, offsets, eig_offsets,
+                                                      int(total_elements), A, eigenvalues, grad_eigenvalues, grad_A,
+                                                      work, flag, stream))
+
+
+def tokura_get_zgeev_ragged_backward_workspacesize(batch_count: int, total_elements: int) -> int:
+    return int(lib().tokura_get_zgeev_ragged_backward_workspacesize(int(batch_count), int(total_elements)))
+
+
+def zgeev_backward(A, eigenvalues, grad_eigenvalues, handle: Handle | None = None, work=None, stream=None):
+    """grad_A for a batch ``A[..., n, n]`` (torch's complex-gradient convention). Returns (grad_A, flag)."""
+    import torch
+
+    n = A.shape[-1]
+    Ab = A.reshape(-1, n, n).contiguous()
+    batch = Ab.shape[0]
+    lam = eigenvalues.reshape(batch, n).contiguous()
+    g = grad_eigenvalues.reshape(batch, n).to(torch.complex128).contiguous()
+    gA = torch.empty_like(Ab)
+    flag = torch.empty(batch, dtype=torch.int8, device=A.device)
+    if batch == 0:
+        return gA.reshape(A.shape), flag
+    need = tokura_get_zgeev_backward_workspacesize(n, batch)
+    if work is None or work.numel() * work.element_size() < need:
+        work = torch.empty(need, dtype=torch.uint8, device=A.device)
+    s = stream if stream is not None else torch.cuda.current_stream(A.device)
+    h = handle if handle is not None else default_handle()
+    st = tokura_zgeev_backward_gpu(h, n, batch, Ab.data_ptr(), lam.data_ptr(), g.data_ptr(), gA.data_ptr(),
+                                   work.data_ptr(), flag.data_ptr(), s.cuda_stream)
+    if st != 0:
+        raise RuntimeError(f"tokura_zgeev_backward_gpu returned {st}")
+    return gA.reshape(A.shape), flag

@@ -31,6 +31,7 @@ SOURCES = [
     "zgeev_noalloc.cu",
     "zgeev_ragged.cu",
     "tokura_tuner.cu",
+    "zgeev_backward.cu",
     "tokura_capi.cpp",
     "compat_cxx.cpp",
 ]

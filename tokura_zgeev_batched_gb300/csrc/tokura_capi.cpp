@@ -122,3 +122,60 @@ extern "C" int tokuraSetRaggedLanes(tokurablas_t* handle, int lanes_per_matrix) 
   handle->ragged_lanes = lanes_per_matrix;
   return 0;
 }
+
+extern "C" size_t tokura_get_zgeev_backward_workspacesize(int n, int batch_count) {
+  if (!(0 < n && n <= TOKURA_ZGEEV_BATCHED_MAX_MATRIX_SIZE)) return (size_t)-1;
+  if (!(0 < batch_count)) return (size_t)-2;
+  return tzg::backward_workspace_bytes(n, batch_count);
+}
+
+extern "C" int tokura_zgeev_backward_gpu(tokurablas_t* handle, int n, int batch_count, const cuDoubleComplex* A,
+                                         const cuDoubleComplex* eigenvalues, const cuDoubleComplex* grad_eigenvalues,
+                                         cuDoubleComplex* grad_A, void* work, char* flag, cudaStream_t stream) {
+  if (handle == nullptr) return -1;
+  if (!(n > 0 && n <= TOKURA_ZGEEV_BATCHED_MAX_MATRIX_SIZE)) return -2;
+  if (A == nullptr) return -3;
+  if (eigenvalues == nullptr || grad_eigenvalues == nullptr) return -4;
+  if (work == nullptr) return -5;
+  if (!(batch_count > 0)) return -6;
+  if (flag == nullptr) return -7;
+  if (grad_A == nullptr) return -8;
+  const int lanes = tzg::plain_config_for(handle, n, batch_count).lanes;
+  const int itmax = handle->itmax_override > 0 ? handle->itmax_override : tzg::default_itmax(n);
+  const cudaError_t err = tzg::launch_backward(
+      lanes, n, batch_count, reinterpret_cast<const double2*>(A), reinterpret_cast<const double2*>(eigenvalues),
+      reinterpret_cast<const double2*>(grad_eigenvalues), reinterpret_cast<double2*>(grad_A),
+      static_cast<double2*>(work), flag, itmax, stream);
+  return err == cudaSuccess ? 0 : 1;
+}
+
+extern "C" size_t tokura_get_zgeev_ragged_backward_workspacesize(int batch_count, long long total_elements) {
+  if (!(batch_count > 0)) return (size_t)-2;
+  if (!(total_elements > 0)) return (size_t)-3;
+  return tzg::ragged_backward_workspace_bytes(batch_count, total_elements);
+}
+
+extern "C" int tokura_zgeev_ragged_backward_gpu(tokurablas_t* handle, int batch_count, const int* n,
+                                                const long long* offsets, const long long* eig_offsets,
+                                                long long total_elements, const cuDoubleComplex* A,
+                                                const cuDoubleComplex* eigenvalues,
+                                                const cuDoubleComplex* grad_eigenvalues, cuDoubleComplex* grad_A,
+                                                void* work, char* flag, cudaStream_t stream) {
+  if (handle == nullptr) return -1;
+  if (n == nullptr) return -2;
+  if (A == nullptr) return -3;
+  if (eigenvalues == nullptr || grad_eigenvalues == nullptr) return -4;
+  if (work == nullptr) return -5;
+  if (!(batch_count > 0)) return -6;
+  if (flag == nullptr) return -7;
+  if (offsets == nullptr) return -8;
+  if (!(total_elements > 0)) return -9;
+  if (grad_A == nullptr) return -10;
+  const int lanes = tzg::ragged_lanes_for(handle, batch_count);
+  const cudaError_t err = tzg::launch_ragged_backward(
+      lanes, handle->sm_count, batch_count, n, offsets, eig_offsets, total_elements,
+      reinterpret_cast<const double2*>(A), reinterpret_cast<const double2*>(eigenvalues),
+      reinterpret_cast<const double2*>(grad_eigenvalues), reinterpret_cast<double2*>(grad_A), work, flag,
+      handle->itmax_override, stream);
+  return err == cudaSuccess ? 0 : 1;
+}

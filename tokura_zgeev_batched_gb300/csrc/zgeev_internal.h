@@ -27,4 +27,14 @@ cudaError_t launch_ragged(int lanes, int sms, int batch, const int* n, const lon
                           const long long* eig_offsets, long long total_elements, const double2* A, double2* eig,
                           void* work, char* flag, int itmax_override, cudaStream_t stream);
 
+// Backward (Abar from A, eigenvalues and their gradients).
+size_t backward_workspace_bytes(int n, int batch);
+cudaError_t launch_backward(int lanes, int n, int batch, const double2* A, const double2* lam, const double2* gbar,
+                            double2* gA, double2* work, char* flag, int itmax, cudaStream_t stream);
+size_t ragged_backward_workspace_bytes(int batch, long long total_elements);
+cudaError_t launch_ragged_backward(int lanes, int sms, int batch, const int* n, const long long* offsets,
+                                   const long long* eig_offsets, long long total_elements, const double2* A,
+                                   const double2* lam, const double2* gbar, double2* gA, void* work, char* flag,
+                                   int itmax_override, cudaStream_t stream);
+
 }  // namespace tzg

@@ -107,8 +107,10 @@ __device__ __forceinline__ void reflect_vectors(double2* const (&p)[NV], const d
 // Householder reduction to upper Hessenberg form, in place. The reflector for
 // column r is P = I - tau v v^H with v[0] = 1, tau real, stored below the
 // subdiagonal of column r (v[1..]). Algorithmic FP64 work ~ (20/3) n^3 ops.
+// If tau_out is given, tau of column r is written to tau_out[r * tau_stride].x
+// (0 for columns that needed no reflector), for forming Q later.
 template <int L>
-__device__ void hessenberg(const MatView& M, const Group<L>& G) {
+__device__ void hessenberg(const MatView& M, const Group<L>& G, double2* tau_out = nullptr, int tau_stride = 0) {
   const int n = M.n;
   const int rs = M.rs;
   const int cs = n * rs;  // column stride
@@ -121,7 +123,10 @@ __device__ void hessenberg(const MatView& M, const Group<L>& G) {
       s2 = fma(z.x, z.x, fma(z.y, z.y, s2));
     }
     s2 = G.sum(s2);
-    if (s2 == 0.0) continue;  // column already in Hessenberg form (group-uniform)
+    if (s2 == 0.0) {  // column already in Hessenberg form (group-uniform)
+      if (tau_out != nullptr && G.rank == 0) tau_out[r * tau_stride] = make_double2(0.0, 0.0);
+      continue;
+    }
     const double2 x0 = x[0];
     const double a0sq = fma(x0.x, x0.x, x0.y * x0.y);
     const double tot = a0sq + s2;
@@ -146,7 +151,10 @@ __device__ void hessenberg(const MatView& M, const Group<L>& G) {
     }
     for (int i = 1 + G.rank; i < m; i += L) x[i * rs] = cmul(x[i * rs], cg);
     G.sync();
-    if (G.rank == 0) x[0] = alpha;
+    if (G.rank == 0) {
+      x[0] = alpha;
+      if (tau_out != nullptr) tau_out[r * tau_stride] = make_double2(tau, 0.0);
+    }
     // Left update: H[r+1:, c] -= tau v (v^H H[r+1:, c]) for c = r+1 .. n-1, two columns at a time.
     {
       int c = r + 1 + G.rank;

@@ -16,6 +16,7 @@
 //               warp do identical amounts of Hessenberg work, and long tiles
 //               are issued first so uneven QR iteration counts and sizes do
 //               not leave SMs idle at the end.
+#include "zgeev_backward.cuh"
 #include "zgeev_internal.h"
 #include "zgeev_lane.cuh"
 
@@ -48,10 +49,12 @@ struct RaggedLayout {
 
 static inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
-static RaggedLayout ragged_layout(int batch, long long total_elements) {
+// `regions` staging areas of total_elements entries: 1 for the forward, 4 for
+// the backward (T, Q, XY and the per-matrix vectors).
+static RaggedLayout ragged_layout(int batch, long long total_elements, int regions = 1) {
   RaggedLayout l;
   l.stage_off = 0;
-  l.plan_off = align256(l.stage_off + sizeof(double2) * (size_t)total_elements);
+  l.plan_off = align256(l.stage_off + sizeof(double2) * (size_t)total_elements * (size_t)regions);
   l.sorted_off = align256(l.plan_off + sizeof(RaggedPlan));
   l.eoff_off = align256(l.sorted_off + sizeof(int) * (size_t)batch);
   l.total = align256(l.eoff_off + sizeof(long long) * (size_t)batch);
@@ -60,6 +63,10 @@ static RaggedLayout ragged_layout(int batch, long long total_elements) {
 
 size_t ragged_workspace_bytes(int batch, long long total_elements) {
   return ragged_layout(batch, total_elements).total;
+}
+
+size_t ragged_backward_workspace_bytes(int batch, long long total_elements) {
+  return ragged_layout(batch, total_elements, 4).total;
 }
 
 __device__ __forceinline__ bool ragged_valid(int nj, long long off, long long total) {
@@ -184,6 +191,48 @@ __global__ void __launch_bounds__(128) zgeev_ragged_kernel(const int* __restrict
   }
 }
 
+// Backward over a ragged batch: same tiles and queue as the forward solver;
+// each matrix's T/Q/XY/vector views sit at the same offset in four regions.
+template <int L>
+__global__ void __launch_bounds__(128) zgeev_ragged_backward_kernel(
+    const int* __restrict__ n, const long long* __restrict__ offsets, const long long* __restrict__ eoff,
+    const double2* __restrict__ A, const double2* __restrict__ lam, const double2* __restrict__ gbar,
+    double2* __restrict__ gA, double2* __restrict__ stage, long long region, char* __restrict__ flag,
+    RaggedPlan* plan, const int* __restrict__ sorted, int itmax_override) {
+  constexpr int TW = 32 / L;
+  const int lane = threadIdx.x & 31;
+  const int slot = lane / L;
+  const int num_tiles = plan->num_tiles;
+  for (;;) {
+    int t = 0;
+    if (lane == 0) t = atomicAdd(&plan->ticket, 1);
+    t = __shfl_sync(0xffffffffu, t, 0);
+    if (t >= num_tiles) break;
+    int lo = 0, hi = kMaxN - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (plan->bins[mid].tile_start <= t) lo = mid; else hi = mid - 1;
+    }
+    const RaggedBin& bin = plan->bins[lo];
+    const int nb = bin.n;
+    const int u = t - bin.tile_start;
+    const int tw = min(TW, bin.count - u * TW);
+    if (slot < tw) {
+      const Group<L> G;
+      const int j = sorted[bin.first + u * TW + slot];
+      const long long nn = (long long)nb * nb;
+      double2* base = stage + bin.stage + (long long)u * TW * nn + slot;
+      BwdViews V{MatView{base, nb, tw}, MatView{base + region, nb, tw}, MatView{base + 2 * region, nb, tw},
+                 base + 3 * region, tw};
+      const int itmax = itmax_override > 0 ? itmax_override : default_itmax(nb);
+      const int status =
+          backward_matrix<L>(A + offsets[j], lam + eoff[j], gbar + eoff[j], gA + offsets[j], V, G, itmax);
+      if (G.rank == 0) flag[j] = (char)status;
+    }
+    __syncwarp();
+  }
+}
+
 template <int L>
 static cudaError_t launch_ragged_solver(int sms, const int* n, const long long* offsets, const long long* eoff,
                                         const double2* A, double2* eig, double2* stage, char* flag, RaggedPlan* plan,
@@ -197,12 +246,12 @@ static cudaError_t launch_ragged_solver(int sms, const int* n, const long long* 
   return cudaGetLastError();
 }
 
-cudaError_t launch_ragged(int lanes, int sms, int batch, const int* n, const long long* offsets,
-                          const long long* eig_offsets, long long total_elements, const double2* A, double2* eig,
-                          void* work, char* flag, int itmax_override, cudaStream_t stream) {
-  const RaggedLayout lay = ragged_layout(batch, total_elements);
+// Device-side planning shared by the forward and backward ragged solvers.
+static cudaError_t ragged_prepare(int lanes, int sms, int batch, const int* n, const long long* offsets,
+                                  const long long* eig_offsets, long long total_elements, const RaggedLayout& lay,
+                                  void* work, char* flag, cudaStream_t stream, RaggedPlan** plan_out,
+                                  int** sorted_out, const long long** eoff_out) {
   char* w = static_cast<char*>(work);
-  double2* stage = reinterpret_cast<double2*>(w + lay.stage_off);
   RaggedPlan* plan = reinterpret_cast<RaggedPlan*>(w + lay.plan_off);
   int* sorted = reinterpret_cast<int*>(w + lay.sorted_off);
   long long* eoff = reinterpret_cast<long long*>(w + lay.eoff_off);
@@ -219,7 +268,30 @@ cudaError_t launch_ragged(int lanes, int sms, int batch, const int* n, const lon
     ragged_scan_kernel<<<1, 1024, 0, stream>>>(batch, n, eoff);
     eo = eoff;
   }
-  if ((err = cudaGetLastError()) != cudaSuccess) return err;
+  *plan_out = plan;
+  *sorted_out = sorted;
+  *eoff_out = eo;
+  return cudaGetLastError();
+}
+
+template <typename Kernel>
+static int persistent_blocks(Kernel k, int sms) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 128, 0) != cudaSuccess || per_sm < 1) per_sm = 1;
+  return sms * per_sm;
+}
+
+cudaError_t launch_ragged(int lanes, int sms, int batch, const int* n, const long long* offsets,
+                          const long long* eig_offsets, long long total_elements, const double2* A, double2* eig,
+                          void* work, char* flag, int itmax_override, cudaStream_t stream) {
+  const RaggedLayout lay = ragged_layout(batch, total_elements);
+  double2* stage = reinterpret_cast<double2*>(static_cast<char*>(work) + lay.stage_off);
+  RaggedPlan* plan;
+  int* sorted;
+  const long long* eo;
+  cudaError_t err = ragged_prepare(lanes, sms, batch, n, offsets, eig_offsets, total_elements, lay, work, flag,
+                                   stream, &plan, &sorted, &eo);
+  if (err != cudaSuccess) return err;
   switch (lanes) {
     case 1:
       return launch_ragged_solver<1>(sms, n, offsets, eo, A, eig, stage, flag, plan, sorted, itmax_override, stream);
@@ -230,6 +302,37 @@ cudaError_t launch_ragged(int lanes, int sms, int batch, const int* n, const lon
     default:
       return cudaErrorInvalidValue;
   }
+}
+
+cudaError_t launch_ragged_backward(int lanes, int sms, int batch, const int* n, const long long* offsets,
+                                   const long long* eig_offsets, long long total_elements, const double2* A,
+                                   const double2* lam, const double2* gbar, double2* gA, void* work, char* flag,
+                                   int itmax_override, cudaStream_t stream) {
+  const RaggedLayout lay = ragged_layout(batch, total_elements, 4);
+  double2* stage = reinterpret_cast<double2*>(static_cast<char*>(work) + lay.stage_off);
+  RaggedPlan* plan;
+  int* sorted;
+  const long long* eo;
+  cudaError_t err = ragged_prepare(lanes, sms, batch, n, offsets, eig_offsets, total_elements, lay, work, flag,
+                                   stream, &plan, &sorted, &eo);
+  if (err != cudaSuccess) return err;
+  switch (lanes) {
+    case 1:
+      zgeev_ragged_backward_kernel<1><<<persistent_blocks(zgeev_ragged_backward_kernel<1>, sms), 128, 0, stream>>>(
+          n, offsets, eo, A, lam, gbar, gA, stage, total_elements, flag, plan, sorted, itmax_override);
+      break;
+    case 2:
+      zgeev_ragged_backward_kernel<2><<<persistent_blocks(zgeev_ragged_backward_kernel<2>, sms), 128, 0, stream>>>(
+          n, offsets, eo, A, lam, gbar, gA, stage, total_elements, flag, plan, sorted, itmax_override);
+      break;
+    case 4:
+      zgeev_ragged_backward_kernel<4><<<persistent_blocks(zgeev_ragged_backward_kernel<4>, sms), 128, 0, stream>>>(
+          n, offsets, eo, A, lam, gbar, gA, stage, total_elements, flag, plan, sorted, itmax_override);
+      break;
+    default:
+      return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
 }
 
 }  // namespace tzg
