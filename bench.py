@@ -194,6 +194,11 @@ def run_reference(args):
 
 # ----------------------------------------------------------------------------- our arm
 
+def phase(name: str) -> None:
+    """Progress marker on stderr (the JSON line is the only stdout output)."""
+    print(f"[bench {time.strftime('%H:%M:%S')}] {name}", file=sys.stderr, flush=True)
+
+
 def time_ms(fn, reps: int, stream) -> float:
     """Average CUDA-event time of fn() on `stream` over reps calls (after one warm-up call)."""
     import torch
@@ -225,6 +230,174 @@ def measure_config1(h, dev, stream, peak, call) -> dict:
     rate = batch / (ms * 1e-3)
     return {"n": n, "batch": batch, "ms": ms, "matrices_per_s": rate, "fp64_frac": flops_per_matrix(n) * rate / peak,
             "lanes_per_matrix": h.plain_config(n, batch)[0], "flagged": int((flag != 0).sum().item())}
+
+
+def measure_config4(h, dev, stream, peak, batch: int = 50000) -> dict:
+    """Differentiable eigenvalues: 50,000 separated-spectrum matrices each at n=16 and n=48.
+
+    Loss L = sum_i exp(Re lambda_i) + |lambda_i|^2, so gbar = exp(Re lambda) + 2 lambda
+    (torch's convention). Times the forward call and the backward call separately
+    (CUDA events); a 16-matrix sample of the gradient is checked against
+    torch.linalg.eigvals' backward on the CPU.
+    """
+    import numpy as np
+    import torch
+
+    from tokura_zgeev_batched_gb300 import api, workloads
+
+    out = {}
+    s = stream.cuda_stream
+    for n in (16, 48):
+        A, _ = workloads.torch_vdv_separated(batch, n, seed=SEED + 40 + n, min_sep=0.05, device=str(dev))
+        eig = torch.empty(batch, n, dtype=torch.complex128, device=dev)
+        flag = torch.empty(batch, dtype=torch.int8, device=dev)
+        work = torch.empty(api.tokura_get_zgeeveigenvaluesgetworspacesize(n, batch), dtype=torch.uint8, device=dev)
+        gA = torch.empty_like(A)
+        bflag = torch.empty(batch, dtype=torch.int8, device=dev)
+        bwork = torch.empty(api.tokura_get_zgeev_backward_workspacesize(n, batch), dtype=torch.uint8, device=dev)
+
+        def fwd():
+            assert api.tokura_zgeev_batched_gpu(h, n, batch, A.data_ptr(), eig.data_ptr(), work.data_ptr(),
+                                                flag.data_ptr(), s) == 0
+
+        fwd()
+        gbar = (torch.exp(eig.real) + 2 * eig).contiguous()
+
+        def bwd():
+            assert api.tokura_zgeev_backward_gpu(h, n, batch, A.data_ptr(), eig.data_ptr(), gbar.data_ptr(),
+                                                 gA.data_ptr(), bwork.data_ptr(), bflag.data_ptr(), s) == 0
+
+        ms_f = time_ms(fwd, 3, stream)
+        ms_b = time_ms(bwd, 3, stream)
+        # gradient spot check against torch.linalg.eigvals backward (CPU, FP64)
+        idx = torch.arange(0, batch, batch // 16, device=dev)[:16]
+        Ac = A[idx].cpu().requires_grad_(True)
+        lam = torch.linalg.eigvals(Ac)
+        torch.sum(torch.exp(lam.real) + lam.real ** 2 + lam.imag ** 2).backward()
+        ref = Ac.grad.numpy()
+        got = gA[idx].cpu().numpy()
+        rel = float(np.max(np.linalg.norm(got - ref, axis=(1, 2)) / np.linalg.norm(ref, axis=(1, 2))))
+        f_fwd = 40.0 * n ** 3
+        f_bwd = 132.0 * n ** 3
+        out[str(n)] = {
+            "batch": batch, "ms_forward": ms_f, "ms_backward": ms_b,
+            "matrices_per_s_forward": batch / (ms_f * 1e-3),
+            "matrices_per_s_fwd_bwd": batch / ((ms_f + ms_b) * 1e-3),
+            "fwd_bwd_over_fwd": (ms_f + ms_b) / ms_f,
+            "fp64_frac_fwd_bwd": (f_fwd + f_bwd) * batch / ((ms_f + ms_b) * 1e-3) / peak,
+            "grad_rel_err_vs_torch_cpu_16": rel,
+            "flagged_forward": int((flag != 0).sum().item()), "flagged_backward": int((bflag != 0).sum().item()),
+        }
+        del A, eig, flag, work, gA, bflag, bwork, gbar
+        torch.cuda.empty_cache()
+    out["convention"] = "F_fwd = 40 n^3, F_bwd = 132 n^3 flop per matrix"
+    return out
+
+
+def measure_config5(h, dev, stream, peak, batch: int = 20000, steps: int = 100) -> dict:
+    """Ragged fwd+bwd optimisation loop in one CUDA graph.
+
+    20,000 matrices, n ~ U{8..64}, separated spectra (min gap 0.05) shifted by +0.5;
+    per matrix the smoothed spectral abscissa tau*logsumexp(Re lambda / tau),
+    tau = 0.05, summed over matrices; 100 gradient-descent steps (lr 1e-2).
+    One step (ragged forward, loss, ragged backward, update) is captured in a
+    CUDA graph and replayed.
+    """
+    import numpy as np
+    import torch
+
+    from tokura_zgeev_batched_gb300 import api, workloads
+    from tokura_zgeev_batched_gb300.autograd import eigvals_ragged
+
+    tau, lr = 0.05, 1e-2
+    ns = workloads.ragged_sizes(batch, 8, 64, seed=SEED + 5)
+    order = np.argsort(ns, kind="stable")
+    sizes_sorted = ns[order].astype(np.int64) ** 2
+    start_sorted = np.concatenate([[0], np.cumsum(sizes_sorted)[:-1]])
+    offsets = np.empty(batch, np.int64)
+    offsets[order] = start_sorted
+    total = int(sizes_sorted.sum())
+    A0 = torch.empty(total, dtype=torch.complex128, device=dev)
+    pos = 0
+    for k in range(8, 65):
+        c = int(np.count_nonzero(ns == k))
+        if c == 0:
+            continue
+        Ak, _ = workloads.torch_vdv_separated(c, k, seed=SEED + 500 + k, min_sep=0.05, shift=0.5, device=str(dev))
+        A0[pos:pos + c * k * k] = Ak.reshape(-1)
+        pos += c * k * k
+    n_d = torch.from_numpy(ns).to(dev)
+    o_d = torch.from_numpy(offsets).to(dev)
+    total_eig = int(ns.sum())
+    seg = torch.repeat_interleave(torch.arange(batch, device=dev), n_d.to(torch.int64))
+    work_f = torch.empty(api.tokura_get_zgeev_ragged_workspacesize(batch, total), dtype=torch.uint8, device=dev)
+    work_b = torch.empty(api.tokura_get_zgeev_ragged_backward_workspacesize(batch, total), dtype=torch.uint8,
+                         device=dev)
+    A = A0.clone().requires_grad_(True)
+
+    def eig_of(X):
+        return eigvals_ragged(X, n_d, o_d, handle=h, work_fwd=work_f, work_bwd=work_b, total_eigenvalues=total_eig)
+
+    def class_max(lam):
+        """Per size class: max, mean and median over matrices of max Re lambda."""
+        re = lam.real
+        m = torch.full((batch,), -float("inf"), dtype=torch.float64, device=dev).scatter_reduce(
+            0, seg, re, reduce="amax")
+        res = {}
+        for lo_, hi_ in ((8, 16), (16, 32), (32, 48), (48, 65)):
+            sel = m[(n_d >= lo_) & (n_d < hi_)]
+            res[f"{lo_}-{min(hi_, 64)}"] = {"max": float(sel.max().item()), "mean": float(sel.mean().item()),
+                                            "median": float(sel.median().item())}
+        return res
+
+    def step():
+        lam = eig_of(A)
+        x = lam.real / tau
+        m = torch.full((batch,), -float("inf"), dtype=torch.float64, device=dev).scatter_reduce(
+            0, seg, x.detach(), reduce="amax")
+        ssum = torch.zeros(batch, dtype=torch.float64, device=dev).index_add(0, seg, torch.exp(x - m[seg]))
+        loss = (tau * (torch.log(ssum) + m)).sum()
+        (g,) = torch.autograd.grad(loss, A)
+        with torch.no_grad():
+            A.sub_(lr * g)
+        return loss
+
+    with torch.no_grad():
+        before = class_max(api.zgeev_ragged(A.detach(), n_d, offsets=o_d, handle=h, work=work_f,
+                                            total_eigenvalues=total_eig)[0])
+    side = torch.cuda.Stream(dev)
+    side.wait_stream(stream)
+    with torch.cuda.stream(side):
+        for _ in range(2):
+            step()
+    stream.wait_stream(side)
+    graph = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(graph):
+        static_loss = step()
+    with torch.no_grad():
+        A.copy_(A0)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        graph.replay()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    final_loss = float(static_loss.item())
+    with torch.no_grad():
+        lam_final, flag = api.zgeev_ragged(A.detach(), n_d, offsets=o_d, handle=h, work=work_f,
+                                           total_eigenvalues=total_eig)
+        after = class_max(lam_final)
+    ms_fwd = time_ms(lambda: api.zgeev_ragged(A.detach(), n_d, offsets=o_d, handle=h, work=work_f,
+                                              total_eigenvalues=total_eig), 3, stream)
+    del graph
+    return {"batch": batch, "steps": steps, "ms_total": ms, "ms_per_step": ms / steps,
+            "matrices_per_s_fwd_bwd": batch * steps / (ms * 1e-3), "ms_forward_only": ms_fwd,
+            "fwd_bwd_over_fwd": (ms / steps) / ms_fwd, "max_re_lambda_before": before,
+            "max_re_lambda_after": after, "final_loss": final_loss,
+            "flagged_after": int((flag != 0).sum().item())}
 
 
 def measure_ragged(h, dev, stream, peak, batch: int = 200000) -> dict:
@@ -387,6 +560,14 @@ def run_ours(args):
     value = ws * BATCH / (ms_step * 1e-3)
     flagged = int((flag != 0).sum().item())
 
+    phase("main timed region done")
+    # Config 3 (ragged) next, while the process state matches a fresh run.
+    ragged = None
+    if not args.no_ragged:
+        # The main buffers stay allocated; the ragged batch needs ~9 GB more.
+        ragged = measure_ragged(h, dev, stream, peak)
+        phase("ragged done")
+
     # Parity spot check of the timed output against LAPACK (rank 0, outside timing).
     parity = None
     if rank == 0 and not args.no_check:
@@ -419,6 +600,7 @@ def run_ours(args):
     roofline["hbm"] = {"achieved": alg_gbs, "peak": hbm_peak, "unit": "GB/s",
                        "frac": (alg_gbs / hbm_peak) if hbm_peak else None}
 
+    phase("parity spot check done")
     # ---- end to end: host buffers through the public API, copies inside every step
     e2e = None
     if not args.no_e2e:
@@ -459,6 +641,7 @@ def run_ours(args):
     del A, eig, flag, work
     torch.cuda.empty_cache()
 
+    phase("e2e done")
     # ---- size sweep (the other orders of the 4 GiB size-sweep configuration)
     sweep = {}
     if not args.no_sweep:
@@ -485,12 +668,17 @@ def run_ours(args):
         sweep[str(N)] = {"batch": BATCH, "matrices_per_s": value / ws, "fp64_frac": achieved / peak,
                          "flagged": flagged}
 
-    ragged = None
-    if not args.no_ragged:
-        ragged = measure_ragged(h, dev, stream, peak)
     config1 = None
     if not args.no_sweep:
         config1 = measure_config1(h, dev, stream, peak, call)
+    phase("sweep and config 1 done")
+    config4 = config5 = None
+    if not args.no_grad:
+        config4 = measure_config4(h, dev, stream, peak)
+        torch.cuda.empty_cache()
+        phase("config 4 done")
+        config5 = measure_config5(h, dev, stream, peak)
+        phase("config 5 done")
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -507,7 +695,8 @@ def run_ours(args):
                        "lanes_per_matrix": h.plain_config(N, BATCH)[0]},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
             "gpu_launches": args.steps, "flagged": flagged, "parity_spot_check": parity, "sweep": sweep,
-            "config1_n32_10000": config1, "ragged": ragged,
+            "config1_n32_10000": config1, "ragged": ragged, "config4_backward": config4,
+            "config5_ragged_gd_graph": config5,
         }
         print(json.dumps(out), flush=True)
     if dist is not None:
@@ -525,6 +714,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-check", action="store_true")
     ap.add_argument("--no-ragged", action="store_true")
+    ap.add_argument("--no-grad", action="store_true")
     ap.add_argument("--n", type=int, default=N, help="matrix order of the timed workload (profiling cases)")
     ap.add_argument("--batch", type=int, default=0, help="matrices per GPU (default: 4 GiB of input)")
     args = ap.parse_args()

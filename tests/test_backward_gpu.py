@@ -111,3 +111,75 @@ def test_ragged_backward_matches_torch(cuda):
         g_ref = torch_cpu_grad(m[None])[0]
         gj = g[offs[j]:offs[j] + k * k].reshape(k, k)
         assert np.linalg.norm(gj - g_ref) <= 1e-9 * max(np.linalg.norm(g_ref), 1.0), (j, k)
+
+
+@pytest.mark.parametrize("lanes", [1, 2, 4])
+def test_ragged_backward_large_shifted(cuda, lanes):
+    """n up to 64, spectra shifted by +0.5 (the optimisation-loop construction), each lane width."""
+    import torch
+
+    from tokura_zgeev_batched_gb300.autograd import eigvals_ragged
+
+    rng = np.random.default_rng(40 + lanes)
+    ns = rng.integers(8, 65, 24).astype(np.int32)
+    mats = [wl.vdv(1, int(k), seed=2000 + j, min_sep=0.05, shift=0.5)[0] for j, k in enumerate(ns)]
+    buf, ns, offs, eoffs = wl.pack_ragged(mats)
+    h = api.Handle()
+    assert h.set_ragged_lanes(lanes) == 0
+    A = torch.from_numpy(buf).cuda().requires_grad_(True)
+    lam = eigvals_ragged(A, torch.from_numpy(ns).cuda(), handle=h)
+    seg = torch.repeat_interleave(torch.arange(len(ns), device="cuda"), torch.from_numpy(ns).cuda().long())
+    tau = 0.05
+    x = lam.real / tau
+    m = torch.full((len(ns),), -float("inf"), dtype=torch.float64, device="cuda").scatter_reduce(
+        0, seg, x.detach(), reduce="amax")
+    ssum = torch.zeros(len(ns), dtype=torch.float64, device="cuda").index_add(0, seg, torch.exp(x - m[seg]))
+    loss = (tau * (torch.log(ssum) + m)).sum()
+    (g,) = torch.autograd.grad(loss, A)
+    g = g.cpu().numpy()
+    for j, mtx in enumerate(mats):
+        k = mtx.shape[0]
+        At = torch.from_numpy(mtx).clone().requires_grad_(True)
+        lt = torch.linalg.eigvals(At)
+        (tau * torch.logsumexp(lt.real / tau, 0)).backward()
+        ref = At.grad.numpy()
+        gj = g[offs[j]:offs[j] + k * k].reshape(k, k)
+        assert np.linalg.norm(gj - ref) <= 1e-8 * max(np.linalg.norm(ref), 1.0), (j, k, lanes)
+
+
+def test_gradient_descent_loop_matches_torch_cpu(cuda):
+    """Ten steps of the smoothed-abscissa descent: GPU ragged fwd+bwd loop vs the same loop in torch on the CPU."""
+    import torch
+
+    from tokura_zgeev_batched_gb300.autograd import eigvals_ragged
+
+    rng = np.random.default_rng(8)
+    ns = rng.integers(8, 30, 12).astype(np.int32)
+    mats = [wl.vdv(1, int(k), seed=3000 + j, min_sep=0.05, shift=0.5)[0] for j, k in enumerate(ns)]
+    buf, ns, offs, eoffs = wl.pack_ragged(mats)
+    tau, lr, steps = 0.05, 1e-2, 10
+    n_d = torch.from_numpy(ns).cuda()
+    seg = torch.repeat_interleave(torch.arange(len(ns), device="cuda"), n_d.long())
+    A = torch.from_numpy(buf).cuda().requires_grad_(True)
+    for _ in range(steps):
+        lam = eigvals_ragged(A, n_d)
+        x = lam.real / tau
+        m = torch.full((len(ns),), -float("inf"), dtype=torch.float64, device="cuda").scatter_reduce(
+            0, seg, x.detach(), reduce="amax")
+        s = torch.zeros(len(ns), dtype=torch.float64, device="cuda").index_add(0, seg, torch.exp(x - m[seg]))
+        (g,) = torch.autograd.grad((tau * (torch.log(s) + m)).sum(), A)
+        with torch.no_grad():
+            A.sub_(lr * g)
+    gpu = A.detach().cpu().numpy()
+    for j, mtx in enumerate(mats):
+        k = mtx.shape[0]
+        # The library sees the buffer column-major, i.e. the matrix mtx^T; eigenvalues agree and the
+        # gradient of the buffer is the gradient w.r.t. mtx in row-major order.
+        X = torch.from_numpy(mtx.copy()).requires_grad_(True)
+        for _ in range(steps):
+            lt = torch.linalg.eigvals(X)
+            (gx,) = torch.autograd.grad(tau * torch.logsumexp(lt.real / tau, 0), X)
+            with torch.no_grad():
+                X.sub_(lr * gx)
+        got = gpu[offs[j]:offs[j] + k * k].reshape(k, k)
+        assert np.abs(got - X.detach().numpy()).max() <= 1e-9 * max(1.0, np.abs(mtx).max()), (j, k)

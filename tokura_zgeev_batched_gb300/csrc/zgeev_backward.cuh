@@ -14,8 +14,13 @@
 //   1. stage + exact pre-scaling, Householder Hessenberg keeping tau (0.74 M);
 //   2. Q from the reflectors by backward accumulation (0.3 M);
 //   3. single-shift QR with full-row/column updates and Q accumulation, with
-//      the forward's eigenvalues as shifts ("perfect shifts": ~1 sweep per
-//      eigenvalue instead of ~3.4; Wilkinson/ad hoc shifts if one misses);
+//      the forward's eigenvalues as shifts ("perfect shifts"; Wilkinson/ad hoc
+//      shifts if one misses). A perfect-shift sweep leaves the bottom
+//      subdiagonal near, but often just above, ulp * |diagonal|; deflating
+//      at kGradDeflationTol = 100 ulp instead (a backward error of ~2e-14 in
+//      T, i.e. ~1e-13 relative in the gradient for separated spectra) brings
+//      the cost to ~1.0 sweep per eigenvalue instead of ~1.75 (~3.4 with
+//      Wilkinson shifts alone);
 //      each deflated T_ii is matched to the nearest unused forward eigenvalue,
 //      whose gradient it takes (~1.8 M);
 //   4. X and Y by triangular back-substitution (0.2 M);
@@ -29,6 +34,9 @@ namespace tzg {
 // Flag: two eigenvalues of T coincide to working precision, so the derivative
 // does not exist; Abar is still returned with the denominators clamped.
 constexpr int kCloseEigenvalues = 4;
+
+// Relative deflation threshold of the gradient's Schur recomputation.
+constexpr double kGradDeflationTol = 100.0 * kUlp;
 
 struct BwdViews {
   MatView T, Q, XY;  // tile-interleaved n x n views (same layout as the forward's staging)
@@ -100,7 +108,7 @@ __device__ int schur_qr(const BwdViews& V, const Group<L>& G, const double2* __r
     for (;;) {
       int hit = lo;
       for (int k = i - G.rank; k > lo; k -= L) {
-        if (negligible_subdiag(T, k, lo, i, smlnum)) {
+        if (negligible_subdiag(T, k, lo, i, smlnum, kGradDeflationTol)) {
           hit = k;
           break;
         }
@@ -151,36 +159,18 @@ __device__ int schur_qr(const BwdViews& V, const Group<L>& G, const double2* __r
       G.sync();
       if (j > lo && G.rank == 0) *T.at(j, j - 1) = rr;
       // Left: rows (j, j+1), columns j .. n-1.
-      for (int c = j + G.rank; c < n; c += L) {
-        double2* pc = T.at(j, c);
-        double2 a = pc[0], b = pc[rs];
-        rot_left(g, a, b);
-        pc[0] = a;
-        pc[rs] = b;
-      }
+      rotate_pairs<false>(g, T.at(j, j + G.rank), strided_count(j + G.rank, n - 1, L), L * cs, rs);
       G.sync();
       // Right: columns (j, j+1), rows 0 .. min(j+1, i); bulge row j+2; and Q's rows 0 .. n-1.
       const int qend = min(j + 1, i);
-      for (int q = G.rank; q <= qend; q += L) {
-        double2* pr = T.at(q, j);
-        double2 a = pr[0], b = pr[cs];
-        rot_right(g, a, b);
-        pr[0] = a;
-        pr[cs] = b;
-      }
+      rotate_pairs<true>(g, T.at(G.rank, j), strided_count(G.rank, qend, L), L * rs, cs);
       if (j + 2 <= i && G.rank == ((j + 2) & (L - 1))) {
         double2* pb = T.at(j + 2, j);
         const double2 b = pb[cs];
         pb[0] = make_double2(fma(g.s.x, b.x, g.s.y * b.y), fma(g.s.x, b.y, -g.s.y * b.x));
         pb[cs] = make_double2(g.c * b.x, g.c * b.y);
       }
-      for (int q = G.rank; q < n; q += L) {
-        double2* pq = Q.at(q, j);
-        double2 a = pq[0], b = pq[cs];
-        rot_right(g, a, b);
-        pq[0] = a;
-        pq[cs] = b;
-      }
+      rotate_pairs<true>(g, Q.at(G.rank, j), strided_count(G.rank, n - 1, L), L * rs, cs);
       G.sync();
     }
   }

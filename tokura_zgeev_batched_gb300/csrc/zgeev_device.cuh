@@ -162,6 +162,34 @@ __device__ __forceinline__ void rot_right(const Rot& g, double2& a, double2& b) 
   b.y = fma(g.c, b0.y, -fma(g.s.x, a0.y, g.s.y * a0.x));
 }
 
+// Applies G (kRight = false: [a; b] <- G [a; b]) or G^H from the right
+// (kRight = true: [a b] <- [a b] G^H) to `count` element pairs p[t*step],
+// p[t*step + pair]. Pair t+1 is loaded before pair t is stored, so memory
+// latency overlaps the 12 FP64 instructions of each pair.
+template <bool kRight>
+__device__ __forceinline__ void rotate_pairs(const Rot& g, double2* p, int count, int step, int pair) {
+  if (count <= 0) return;
+  double2 a = p[0], b = p[pair];
+  for (int t = 1; t < count; ++t) {
+    double2* pn = p + step;
+    const double2 an = pn[0], bn = pn[pair];
+    if (kRight) rot_right(g, a, b); else rot_left(g, a, b);
+    p[0] = a;
+    p[pair] = b;
+    a = an;
+    b = bn;
+    p = pn;
+  }
+  if (kRight) rot_right(g, a, b); else rot_left(g, a, b);
+  p[0] = a;
+  p[pair] = b;
+}
+
+// Number of t >= 0 with first + t*step <= last.
+__device__ __forceinline__ int strided_count(int first, int last, int step) {
+  return first <= last ? (last - first) / step + 1 : 0;
+}
+
 // Eigenvalue of [a b; c d] closest to d (Wilkinson shift), in a scaled,
 // cancellation-free form: d - bc / (x + sqrt(x^2 + bc)), x = (a - d)/2,
 // with the root's sign chosen so that |x + sqrt(.)| is maximal.

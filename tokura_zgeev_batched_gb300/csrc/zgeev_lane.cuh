@@ -186,8 +186,10 @@ __device__ void hessenberg(const MatView& M, const Group<L>& G, double2* tau_out
 
 // Deflation test for subdiagonal entry k (k >= 1) of the active block [lo, hi]:
 // negligible by the Ahues-Tisseur criterion (LAPACK Working Note 122), with
-// smlnum guarding underflow.
-__device__ __forceinline__ bool negligible_subdiag(const MatView& M, int k, int lo, int hi, double smlnum) {
+// smlnum guarding underflow. `tol` is the relative threshold (ulp for the
+// eigenvalue path; the gradient path relaxes it, see zgeev_backward.cuh).
+__device__ __forceinline__ bool negligible_subdiag(const MatView& M, int k, int lo, int hi, double smlnum,
+                                                   double tol = kUlp) {
   const double2 hk = *M.at(k, k - 1);
   const double h1 = cabs1(hk);
   if (h1 <= smlnum) return true;
@@ -198,7 +200,7 @@ __device__ __forceinline__ bool negligible_subdiag(const MatView& M, int k, int 
     if (k - 2 >= lo) tst += cabs1(*M.at(k - 1, k - 2));
     if (k + 1 <= hi) tst += cabs1(*M.at(k + 1, k));
   }
-  if (h1 > kUlp * tst) return false;
+  if (h1 > tol * tst) return false;
   const double2 up = *M.at(k - 1, k);
   const double hu = cabs1(up);
   const double ab = fmax(h1, hu), ba = fmin(h1, hu);
@@ -206,7 +208,7 @@ __device__ __forceinline__ bool negligible_subdiag(const MatView& M, int k, int 
   const double d1 = cabs1(dkk);
   const double aa = fmax(d1, dd), bb = fmin(d1, dd);
   const double s = aa + ab;
-  return ba * (ab / s) <= fmax(smlnum, kUlp * (bb * (aa / s)));
+  return ba * (ab / s) <= fmax(smlnum, tol * (bb * (aa / s)));
 }
 
 // Single-shift complex QR on the Hessenberg matrix (eigenvalues only), from
@@ -286,26 +288,10 @@ __device__ int qr_eigenvalues(const MatView& M, const Group<L>& G, double2* __re
         const Rot g = make_rot(x, y, rr);
         G.sync();  // all lanes have read the bulge before it is overwritten
         if (j > lo && G.rank == 0) *M.at(j, j - 1) = rr;
-        // Left: rows (j, j+1), columns j .. i (next pair loaded before the current one is stored).
+        // Left: rows (j, j+1), columns j .. i.
         {
           const int c0 = j + G.rank;
-          if (c0 <= i) {
-            double2* pc = M.at(j, c0);
-            double2 a = pc[0], b = pc[rs];
-            for (int c = c0 + L; c <= i; c += L) {
-              double2* pn = pc + L * cs;
-              const double2 an = pn[0], bn = pn[rs];
-              rot_left(g, a, b);
-              pc[0] = a;
-              pc[rs] = b;
-              a = an;
-              b = bn;
-              pc = pn;
-            }
-            rot_left(g, a, b);
-            pc[0] = a;
-            pc[rs] = b;
-          }
+          rotate_pairs<false>(g, M.at(j, c0), strided_count(c0, i, L), L * cs, rs);
         }
         G.sync();
         // Right: columns (j, j+1), rows lo .. min(j+2, i); row j+2 holds the
@@ -313,23 +299,7 @@ __device__ int qr_eigenvalues(const MatView& M, const Group<L>& G, double2* __re
         {
           const int qend = min(j + 1, i);
           const int q0 = lo + G.rank;
-          if (q0 <= qend) {
-            double2* pr = M.at(q0, j);
-            double2 a = pr[0], b = pr[cs];
-            for (int q = q0 + L; q <= qend; q += L) {
-              double2* pn = pr + L * rs;
-              const double2 an = pn[0], bn = pn[cs];
-              rot_right(g, a, b);
-              pr[0] = a;
-              pr[cs] = b;
-              a = an;
-              b = bn;
-              pr = pn;
-            }
-            rot_right(g, a, b);
-            pr[0] = a;
-            pr[cs] = b;
-          }
+          rotate_pairs<true>(g, M.at(q0, j), strided_count(q0, qend, L), L * rs, cs);
           if (j + 2 <= i && G.rank == ((j + 2 - lo) & (L - 1))) {
             double2* pb = M.at(j + 2, j);
             const double2 b = pb[cs];

@@ -151,8 +151,13 @@ __global__ void __launch_bounds__(1024) ragged_scan_kernel(int batch, const int*
   }
 }
 
+// Resident blocks per SM the compiler is asked to allow (register budget).
+#ifndef TZG_RAGGED_MIN_BLOCKS
+#define TZG_RAGGED_MIN_BLOCKS 1
+#endif
+
 template <int L>
-__global__ void __launch_bounds__(128) zgeev_ragged_kernel(const int* __restrict__ n,
+__global__ void __launch_bounds__(128, TZG_RAGGED_MIN_BLOCKS) zgeev_ragged_kernel(const int* __restrict__ n,
                                                            const long long* __restrict__ offsets,
                                                            const long long* __restrict__ eoff,
                                                            const double2* __restrict__ A, double2* __restrict__ eig,

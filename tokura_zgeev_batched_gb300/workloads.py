@@ -143,3 +143,40 @@ def torch_companion(batch: int, n: int, seed: int = SEED, device: str = "cuda"):
 
 
 TORCH_GENERATORS = {"gaussian": torch_gaussian, "vdv": torch_vdv, "companion": torch_companion}
+
+
+def torch_vdv_separated(batch: int, n: int, seed: int = SEED, min_sep: float = 0.05, shift: float = 0.0,
+                        device: str = "cuda", chunk: int = 4096):
+    """A = V diag(lambda) V^-1 (V = I + 0.3 G) with lambda in the unit disk, pairwise >= min_sep apart
+    (rejection-resampled), plus ``shift``. Returns (A, lambda)."""
+    import torch
+
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    A = torch.empty(batch, n, n, dtype=torch.complex128, device=device)
+    lam_all = torch.empty(batch, n, dtype=torch.complex128, device=device)
+    eye = torch.eye(n, dtype=torch.complex128, device=device)
+
+    def disk(b):
+        r = torch.sqrt(torch.rand(b, n, generator=g, device=device, dtype=torch.float64))
+        th = 2 * torch.pi * torch.rand(b, n, generator=g, device=device, dtype=torch.float64)
+        return torch.polar(r, th)
+
+    for s in range(0, batch, chunk):
+        b = min(chunk, batch - s)
+        lam = disk(b)
+        if n > 1 and min_sep > 0:
+            big = torch.eye(n, device=device, dtype=torch.float64) * 10
+            for _ in range(1000):
+                d = (lam[:, :, None] - lam[:, None, :]).abs() + big
+                bad = d.min(dim=-1).values < min_sep
+                if not bool(bad.any()):
+                    break
+                lam = torch.where(bad, disk(b), lam)
+        lam = lam + shift
+        G = torch.complex(torch.randn(b, n, n, generator=g, device=device, dtype=torch.float64),
+                          torch.randn(b, n, n, generator=g, device=device, dtype=torch.float64))
+        V = eye + 0.3 * G
+        A[s:s + b] = torch.linalg.solve(V, V * lam[:, None, :], left=False)
+        lam_all[s:s + b] = lam
+    return A, lam_all
