@@ -232,7 +232,7 @@ def measure_config1(h, dev, stream, peak, call) -> dict:
             "lanes_per_matrix": h.plain_config(n, batch)[0], "flagged": int((flag != 0).sum().item())}
 
 
-def measure_config4(h, dev, stream, peak, batch: int = 50000) -> dict:
+def measure_config4(h, dev, stream, peak, batch: int = 50000, orders=(16, 48)) -> dict:
     """Differentiable eigenvalues: 50,000 separated-spectrum matrices each at n=16 and n=48.
 
     Loss L = sum_i exp(Re lambda_i) + |lambda_i|^2, so gbar = exp(Re lambda) + 2 lambda
@@ -247,7 +247,7 @@ def measure_config4(h, dev, stream, peak, batch: int = 50000) -> dict:
 
     out = {}
     s = stream.cuda_stream
-    for n in (16, 48):
+    for n in orders:
         A, _ = workloads.torch_vdv_separated(batch, n, seed=SEED + 40 + n, min_sep=0.05, device=str(dev))
         eig = torch.empty(batch, n, dtype=torch.complex128, device=dev)
         flag = torch.empty(batch, dtype=torch.int8, device=dev)
@@ -270,7 +270,7 @@ def measure_config4(h, dev, stream, peak, batch: int = 50000) -> dict:
         ms_f = time_ms(fwd, 3, stream)
         ms_b = time_ms(bwd, 3, stream)
         # gradient spot check against torch.linalg.eigvals backward (CPU, FP64)
-        idx = torch.arange(0, batch, batch // 16, device=dev)[:16]
+        idx = torch.arange(0, batch, max(1, batch // 16), device=dev)[:16]
         Ac = A[idx].cpu().requires_grad_(True)
         lam = torch.linalg.eigvals(Ac)
         torch.sum(torch.exp(lam.real) + lam.real ** 2 + lam.imag ** 2).backward()
@@ -703,6 +703,25 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_only(args):
+    """One configuration alone, for small profiling captures (prints its JSON object)."""
+    import torch
+
+    from tokura_zgeev_batched_gb300 import api, build
+
+    build.build()
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    peak = api.probe_fp64_peak(dev)
+    h = api.Handle()
+    stream = torch.cuda.current_stream(dev)
+    if args.only == "ragged":
+        out = measure_ragged(h, dev, stream, peak, batch=args.batch or 200000)
+    else:
+        out = measure_config4(h, dev, stream, peak, batch=args.batch or 50000, orders=(args.n,))
+    print(json.dumps({"only": args.only, "result": out}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -715,12 +734,16 @@ def main():
     ap.add_argument("--no-check", action="store_true")
     ap.add_argument("--no-ragged", action="store_true")
     ap.add_argument("--no-grad", action="store_true")
+    ap.add_argument("--only", choices=["ragged", "backward"], default=None,
+                    help="run one configuration alone (profiling cases); --batch sets its size")
     ap.add_argument("--n", type=int, default=N, help="matrix order of the timed workload (profiling cases)")
     ap.add_argument("--batch", type=int, default=0, help="matrices per GPU (default: 4 GiB of input)")
     args = ap.parse_args()
     set_workload(args.n, args.batch)
     if args.impl == "reference":
         run_reference(args)
+    elif args.only is not None:
+        run_only(args)
     else:
         run_ours(args)
 

@@ -123,7 +123,7 @@ def torch_vdv(batch: int, n: int, seed: int = SEED, device: str = "cuda", chunk:
         G = torch.complex(torch.randn(b, n, n, generator=g, device=device, dtype=torch.float64),
                           torch.randn(b, n, n, generator=g, device=device, dtype=torch.float64))
         V = eye + 0.3 * G
-        out[s:s + b] = torch.linalg.solve(V, V * lam[:, None, :], left=False)
+        out[s:s + b] = _solve_right(V, V * lam[:, None, :])
     return out
 
 
@@ -177,6 +177,16 @@ def torch_vdv_separated(batch: int, n: int, seed: int = SEED, min_sep: float = 0
         G = torch.complex(torch.randn(b, n, n, generator=g, device=device, dtype=torch.float64),
                           torch.randn(b, n, n, generator=g, device=device, dtype=torch.float64))
         V = eye + 0.3 * G
-        A[s:s + b] = torch.linalg.solve(V, V * lam[:, None, :], left=False)
+        A[s:s + b] = _solve_right(V, V * lam[:, None, :])
         lam_all[s:s + b] = lam
     return A, lam_all
+
+
+def _solve_right(V, B):
+    """X with X V = B; on the CPU if the GPU linear-algebra library cannot be loaded (e.g. under a profiler)."""
+    import torch
+
+    try:
+        return torch.linalg.solve(V, B, left=False)
+    except RuntimeError:
+        return torch.linalg.solve(V.cpu(), B.cpu(), left=False).to(V.device)
