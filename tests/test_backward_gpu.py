@@ -39,7 +39,7 @@ def our_grad(A_np, lanes=0):
 
 
 @pytest.mark.parametrize("n", [1, 2, 5, 16, 48])
-@pytest.mark.parametrize("lanes", [1, 2, 4])
+@pytest.mark.parametrize("lanes", [1, 2, 4, 8])
 def test_matches_torch_eigvals_backward(cuda, n, lanes):
     A = wl.vdv(24, n, seed=300 + n, min_sep=0.05)
     g_ref = torch_cpu_grad(A)
@@ -113,7 +113,7 @@ def test_ragged_backward_matches_torch(cuda):
         assert np.linalg.norm(gj - g_ref) <= 1e-9 * max(np.linalg.norm(g_ref), 1.0), (j, k)
 
 
-@pytest.mark.parametrize("lanes", [1, 2, 4])
+@pytest.mark.parametrize("lanes", [0, 1, 2, 4, 8])
 def test_ragged_backward_large_shifted(cuda, lanes):
     """n up to 64, spectra shifted by +0.5 (the optimisation-loop construction), each lane width."""
     import torch

@@ -30,7 +30,7 @@ def gpu_eigs(A_np, lanes=0):
     return w.cpu().numpy(), f.cpu().numpy()
 
 
-@pytest.mark.parametrize("lanes", [1, 2, 4])
+@pytest.mark.parametrize("lanes", [1, 2, 4, 8])
 def test_golden_cases(cuda, golden, lanes):
     for name in [str(x) for x in golden["names"]]:
         A = golden[f"{name}/A"]

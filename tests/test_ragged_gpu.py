@@ -30,7 +30,7 @@ def check_against_lapack(mats, eig, eoffs, flag):
     return worst
 
 
-@pytest.mark.parametrize("lanes", [1, 2, 4])
+@pytest.mark.parametrize("lanes", [0, 1, 2, 4, 8])
 def test_ragged_matches_lapack(cuda, lanes):
     import torch
 

@@ -71,7 +71,9 @@ extern "C" int tokuraSetSweepCap(tokurablas_t* handle, int cap) {
 extern "C" int tokuraSetPlainConfig(tokurablas_t* handle, int n, int lanes_per_matrix, int threads_per_block) {
   if (handle == nullptr) return -1;
   if (!(n > 0 && n <= TOKURA_ZGEEV_BATCHED_MAX_MATRIX_SIZE)) return -2;
-  if (!(lanes_per_matrix == 0 || lanes_per_matrix == 1 || lanes_per_matrix == 2 || lanes_per_matrix == 4)) return -3;
+  if (!(lanes_per_matrix == 0 || lanes_per_matrix == 1 || lanes_per_matrix == 2 || lanes_per_matrix == 4 ||
+        lanes_per_matrix == 8))
+    return -3;
   if (!(threads_per_block == 0 || (threads_per_block >= 32 && threads_per_block <= 256 && threads_per_block % 32 == 0)))
     return -4;
   handle->plain[n] = PlainConfig{lanes_per_matrix, threads_per_block};
@@ -108,8 +110,7 @@ extern "C" int tokura_zgeev_ragged_gpu(tokurablas_t* handle, int batch_count, co
   if (flag == nullptr) return -7;
   if (offsets == nullptr) return -8;
   if (!(total_elements > 0)) return -9;
-  const int lanes = tzg::ragged_lanes_for(handle, batch_count);
-  const cudaError_t err = tzg::launch_ragged(lanes, handle->sm_count, batch_count, n, offsets, eig_offsets,
+  const cudaError_t err = tzg::launch_ragged(handle->ragged_lanes, handle->sm_count, batch_count, n, offsets, eig_offsets,
                                              total_elements, reinterpret_cast<const double2*>(A),
                                              reinterpret_cast<double2*>(eigenvalues), work, flag,
                                              handle->itmax_override, stream);
@@ -118,7 +119,9 @@ extern "C" int tokura_zgeev_ragged_gpu(tokurablas_t* handle, int batch_count, co
 
 extern "C" int tokuraSetRaggedLanes(tokurablas_t* handle, int lanes_per_matrix) {
   if (handle == nullptr) return -1;
-  if (!(lanes_per_matrix == 0 || lanes_per_matrix == 1 || lanes_per_matrix == 2 || lanes_per_matrix == 4)) return -3;
+  if (!(lanes_per_matrix == 0 || lanes_per_matrix == 1 || lanes_per_matrix == 2 || lanes_per_matrix == 4 ||
+        lanes_per_matrix == 8))
+    return -3;
   handle->ragged_lanes = lanes_per_matrix;
   return 0;
 }
@@ -171,9 +174,8 @@ extern "C" int tokura_zgeev_ragged_backward_gpu(tokurablas_t* handle, int batch_
   if (offsets == nullptr) return -8;
   if (!(total_elements > 0)) return -9;
   if (grad_A == nullptr) return -10;
-  const int lanes = tzg::ragged_lanes_for(handle, batch_count);
   const cudaError_t err = tzg::launch_ragged_backward(
-      lanes, handle->sm_count, batch_count, n, offsets, eig_offsets, total_elements,
+      handle->ragged_lanes, handle->sm_count, batch_count, n, offsets, eig_offsets, total_elements,
       reinterpret_cast<const double2*>(A), reinterpret_cast<const double2*>(eigenvalues),
       reinterpret_cast<const double2*>(grad_eigenvalues), reinterpret_cast<double2*>(grad_A), work, flag,
       handle->itmax_override, stream);

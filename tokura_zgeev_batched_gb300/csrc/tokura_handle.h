@@ -9,7 +9,7 @@ struct tokurablas_t {
   int itmax_override = 0;  // >0 replaces the per-eigenvalue sweep cap 30*max(10,n)
   // Tuned plain-kernel shape per n (index 1..64); lanes == 0 means "heuristic".
   tzg::PlainConfig plain[65] = {};
-  int ragged_lanes = 0;  // lanes per matrix of the ragged solver; 0 = heuristic
+  int ragged_lanes = 0;  // lanes per matrix of the ragged solvers; 0 = chosen per size bin on the device
 };
 
 namespace tzg {
@@ -42,10 +42,6 @@ inline int lanes_for_batch(const tokurablas_t* h, long long batch) {
   if (batch >= want_lanes) return 1;
   if (batch * 2 >= want_lanes) return 2;
   return 4;
-}
-
-inline int ragged_lanes_for(const tokurablas_t* h, long long batch) {
-  return h->ragged_lanes > 0 ? h->ragged_lanes : lanes_for_batch(h, batch);
 }
 
 }  // namespace tzg

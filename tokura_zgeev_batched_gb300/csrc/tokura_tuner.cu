@@ -97,14 +97,14 @@ extern "C" TOKURA_API int tokuraAutotune(tokurablas_t* handle, int n_min, int n_
   double2* eig = static_cast<double2*>(b.p[1]);
   double2* work = static_cast<double2*>(b.p[2]);
   char* flag = static_cast<char*>(b.p[3]);
-  static const int kLanes[3] = {1, 2, 4};
+  static const int kLanes[4] = {1, 2, 4, 8};
   static const int kThreads[3] = {64, 128, 256};
   for (int n = n_min; n <= n_max; ++n) {
     const long long count = (long long)n * n * batch_count;
     fill_cgauss_kernel<<<handle->sm_count * 4, 256, 0, stream>>>(A, count, 0x5eed0000ULL + n);
     float best = 1e30f;
     PlainConfig best_cfg{1, 128};
-    for (int li = 0; li < 3; ++li) {
+    for (int li = 0; li < 4; ++li) {
       if (n <= 2 && kLanes[li] > 1) continue;
       for (int ti = 0; ti < 3; ++ti) {
         const PlainConfig cfg{kLanes[li], kThreads[ti]};
@@ -145,8 +145,8 @@ extern "C" TOKURA_API int tokuraAutotuneRagged(tokurablas_t* handle, int batch_c
   fill_cgauss_kernel<<<handle->sm_count * 4, 256, 0, stream>>>(A, total, 0x5eed7777ULL);
   fill_sizes_kernel<<<1, 1, 0, stream>>>(n, off, batch_count, n_min, n_max, 0x5eed1234ULL);
   float best = 1e30f;
-  int best_lanes = 1;
-  for (int lanes : {1, 2, 4}) {
+  int best_lanes = 0;
+  for (int lanes : {0, 1, 2, 4, 8}) {  // 0: lane width chosen per size bin
     cudaError_t err;
     const float ms = time_launches(stream, 2, [&]() {
       return launch_ragged(lanes, handle->sm_count, batch_count, n, off, nullptr, total, A,
@@ -179,7 +179,7 @@ extern "C" TOKURA_API int tokuraSaveTuning(const tokurablas_t* handle, const cha
   for (int n = 1; n <= TOKURA_ZGEEV_BATCHED_MAX_MATRIX_SIZE; ++n)
     if (handle->plain[n].lanes > 0)
       std::fprintf(f, "plain %d %d %d\n", n, handle->plain[n].lanes, handle->plain[n].threads);
-  if (handle->ragged_lanes > 0) std::fprintf(f, "ragged %d\n", handle->ragged_lanes);
+  std::fprintf(f, "ragged %d\n", handle->ragged_lanes);
   return std::fclose(f) == 0 ? 0 : 1;
 }
 
@@ -207,13 +207,13 @@ extern "C" TOKURA_API int tokuraLoadTuning(tokurablas_t* handle, const char* pat
     if (std::strcmp(word, "plain") == 0) {
       int n, lanes, threads;
       if (std::fscanf(f, "%d %d %d", &n, &lanes, &threads) != 3 || n < 1 || n > 64 ||
-          !(lanes == 1 || lanes == 2 || lanes == 4) || threads < 32 || threads > 256 || threads % 32) {
+          !(lanes == 1 || lanes == 2 || lanes == 4 || lanes == 8) || threads < 32 || threads > 256 || threads % 32) {
         status = 2;
         break;
       }
       table[n] = tzg::PlainConfig{lanes, threads};
     } else if (std::strcmp(word, "ragged") == 0) {
-      if (std::fscanf(f, "%d", &ragged) != 1 || !(ragged == 1 || ragged == 2 || ragged == 4)) {
+      if (std::fscanf(f, "%d", &ragged) != 1 || !(ragged >= 0 && ragged <= 8 && (ragged & (ragged - 1)) == 0)) {
         status = 2;
         break;
       }

@@ -53,6 +53,9 @@ cudaError_t launch_backward(int lanes, int n, int batch, const double2* A, const
     case 4:
       zgeev_backward_kernel<4><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, lam, gbar, gA, work, flag, itmax);
       break;
+    case 8:
+      zgeev_backward_kernel<8><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, lam, gbar, gA, work, flag, itmax);
+      break;
     default:
       return cudaErrorInvalidValue;
   }

@@ -71,6 +71,12 @@ __device__ __forceinline__ int dexp_field(double x) {
 // 2^e as a double for e in the normal range.
 __device__ __forceinline__ double pow2(int e) { return __hiloint2double((e + 1023) << 20, 0); }
 
+// Compile-time lane count tag (for dispatch from a runtime lane width).
+template <int L>
+struct Lanes {
+  static constexpr int value = L;
+};
+
 // Lane group of L consecutive lanes of one warp cooperating on one matrix.
 template <int L>
 struct Group {

@@ -50,6 +50,9 @@ cudaError_t launch_plain(const PlainConfig& cfg, int n, int batch, const double2
     case 4:
       zgeev_plain_kernel<4><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, eig, work, flag, itmax);
       break;
+    case 8:
+      zgeev_plain_kernel<8><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, eig, work, flag, itmax);
+      break;
     default:
       return cudaErrorInvalidValue;
   }
