@@ -33,7 +33,7 @@ METRIC = "matrices/s eigvals (n=32,64; ragged 1-64), fwd+bwd matrices/s, % FP64 
 N = 64
 BATCH = (4 << 30) // (16 * N * N)  # 65,536 matrices = 4 GiB of input
 SEED = 20261203
-SWEEP_NS = (4, 8, 16, 32, 48)
+SWEEP_NS = (4, 8, 16, 32, 48)  # the size sweep's other orders (n = 64 is the timed workload)
 
 
 def set_workload(n: int, batch: int = 0) -> None:
@@ -53,6 +53,22 @@ def bytes_per_matrix(n: int) -> int:
 
 
 # ----------------------------------------------------------------------------- helpers
+
+def max_over_ranks(x: float, dist, device) -> float:
+    """Max of a per-rank scalar over all ranks (identity without torch.distributed)."""
+    if dist is None:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def rank_seed(seed: int, rank: int) -> int:
+    """Each rank solves its own batch (weak scaling: no data is exchanged)."""
+    return seed + 1000 * rank
+
 
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
@@ -199,6 +215,21 @@ def phase(name: str) -> None:
     print(f"[bench {time.strftime('%H:%M:%S')}] {name}", file=sys.stderr, flush=True)
 
 
+def spot_check(A, eig, flag, count: int) -> dict:
+    """Max/p99 of max|dlambda|/||A||_F against LAPACK zgeev on an evenly spaced sample of the batch."""
+    import torch
+
+    from oracle import lapack_oracle as lo
+
+    batch = A.shape[0]
+    idx = torch.arange(0, batch, max(1, batch // count), device=A.device)[:count]
+    rep = lo.parity_report(A[idx].cpu().numpy(), eig[idx].cpu().numpy(), flag[idx].cpu().numpy())
+    return {"checked": int(idx.numel()), "max_rel_err_fro": rep["max_rel_err"], "p99_rel_err_fro": rep["p99_rel_err"],
+            "flag_mismatch": rep["flag_mismatch"], "lapack_fail": rep["lapack_fail"],
+            "cond_le_1e3": rep.get("well_conditioned"), "max_rel_err_fro_cond_le_1e3": rep.get("max_rel_err_well"),
+            "p99_rel_err_fro_cond_le_1e3": rep.get("p99_rel_err_well")}
+
+
 def time_ms(fn, reps: int, stream) -> float:
     """Average CUDA-event time of fn() on `stream` over reps calls (after one warm-up call)."""
     import torch
@@ -229,7 +260,8 @@ def measure_config1(h, dev, stream, peak, call) -> dict:
     ms = time_ms(lambda: call(n, batch, A, eig, flag, work), 5, stream)
     rate = batch / (ms * 1e-3)
     return {"n": n, "batch": batch, "ms": ms, "matrices_per_s": rate, "fp64_frac": flops_per_matrix(n) * rate / peak,
-            "lanes_per_matrix": h.plain_config(n, batch)[0], "flagged": int((flag != 0).sum().item())}
+            "lanes_per_matrix": h.plain_config(n, batch)[0], "flagged": int((flag != 0).sum().item()),
+            "parity": spot_check(A, eig, flag, 256)}
 
 
 def measure_config4(h, dev, stream, peak, batch: int = 50000, orders=(16, 48)) -> dict:
@@ -439,6 +471,22 @@ def measure_ragged(h, dev, stream, peak, batch: int = 200000) -> dict:
 
     ms_ragged = time_ms(ragged_call, 3, stream)
     flagged = int((flag != 0).sum().item())
+    # parity sample: 4 matrices of each order, compared with LAPACK
+    from oracle import lapack_oracle as lo
+
+    eoffs = np.concatenate([[0], np.cumsum(ns.astype(np.int64))[:-1]])
+    eig_h = eig.cpu().numpy()
+    flag_h = flag.cpu().numpy()
+    worst, rels = 0.0, []
+    for k in range(1, 65):
+        js = np.where(ns == k)[0][:4]
+        if len(js) == 0:
+            continue
+        mats = np.stack([A[offsets[j]:offsets[j] + k * k].cpu().numpy().reshape(k, k) for j in js])
+        w = np.stack([eig_h[eoffs[j]:eoffs[j] + k] for j in js])
+        rep = lo.parity_report(mats, w, flag_h[js], with_cond=False)
+        rels.extend(list(rep["rel_err"][np.isfinite(rep["rel_err"])]))
+    parity = {"checked": len(rels), "max_rel_err_fro": float(np.max(rels)), "p99_rel_err_fro": float(np.percentile(rels, 99))}
     # CUDA graph of the ragged call (planning kernels + persistent solver).
     graph_ms = None
     try:
@@ -485,8 +533,8 @@ def measure_ragged(h, dev, stream, peak, batch: int = 200000) -> dict:
     return {"batch": batch, "total_elements": total, "ms_ragged": ms_ragged, "ms_ragged_graph": graph_ms,
             "ms_per_size_plain": ms_plain, "matrices_per_s_ragged": batch / (best * 1e-3),
             "matrices_per_s_per_size_plain": batch / (ms_plain * 1e-3), "speedup_vs_per_size": ms_plain / best,
-            "fp64_frac": work_flops / (best * 1e-3) / peak, "lanes_per_matrix": None, "flagged": flagged,
-            "plain_launches": int(np.count_nonzero(counts))}
+            "fp64_frac": work_flops / (best * 1e-3) / peak, "flagged": flagged,
+            "plain_launches": int(np.count_nonzero(counts)), "parity": parity}
 
 def run_ours(args):
     import numpy as np
@@ -518,7 +566,7 @@ def run_ours(args):
     s = stream.cuda_stream
 
     def alloc(n, batch, gen="gaussian", seed=SEED):
-        A = workloads.TORCH_GENERATORS[gen](batch, n, seed=seed + 1000 * rank, device=str(dev))
+        A = workloads.TORCH_GENERATORS[gen](batch, n, seed=rank_seed(seed, rank), device=str(dev))
         eig = torch.empty(batch, n, dtype=torch.complex128, device=dev)
         flag = torch.empty(batch, dtype=torch.int8, device=dev)
         work = torch.empty(api.tokura_get_zgeeveigenvaluesgetworspacesize(n, batch), dtype=torch.uint8, device=dev)
@@ -550,12 +598,8 @@ def run_ours(args):
     torch.cuda.synchronize()
     barrier()
     clocks = sampler.stop()
-    ms_total = t0.elapsed_time(t1)
+    ms_total = max_over_ranks(t0.elapsed_time(t1), dist, dev)
     kern_ms = [a.elapsed_time(b) for a, b in ev]
-    if dist is not None:
-        tt = torch.tensor([ms_total], device=dev)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        ms_total = float(tt.item())
     ms_step = ms_total / args.steps
     value = ws * BATCH / (ms_step * 1e-3)
     flagged = int((flag != 0).sum().item())
@@ -571,12 +615,7 @@ def run_ours(args):
     # Parity spot check of the timed output against LAPACK (rank 0, outside timing).
     parity = None
     if rank == 0 and not args.no_check:
-        from oracle import lapack_oracle as lo
-
-        idx = torch.arange(0, BATCH, BATCH // 256, device=dev)[:256]
-        rep = lo.parity_report(A[idx].cpu().numpy(), eig[idx].cpu().numpy(), flag[idx].cpu().numpy())
-        parity = {"checked": 256, "max_rel_err_fro": rep["max_rel_err"], "flag_mismatch": rep["flag_mismatch"],
-                  "max_rel_err_fro_cond_le_1e3": rep.get("max_rel_err_well")}
+        parity = spot_check(A, eig, flag, 256)
 
     kern_avg = statistics.mean(kern_ms)
     achieved = flops_per_matrix(N) * BATCH / (kern_avg * 1e-3)
@@ -628,11 +667,7 @@ def run_ours(args):
         e1.record(stream)
         torch.cuda.synchronize()
         barrier()
-        e_ms = e0.elapsed_time(e1) / args.steps
-        if dist is not None:
-            tt = torch.tensor([e_ms], device=dev)
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-            e_ms = float(tt.item())
+        e_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, dist, dev)
         e2e = {"value": ws * BATCH / (e_ms * 1e-3), "unit": "matrices/s",
                "h2d_bytes_per_step": A_host.numel() * 16,
                "d2h_bytes_per_step": eig_host.numel() * 16 + flag_host.numel(),
@@ -645,28 +680,25 @@ def run_ours(args):
     # ---- size sweep (the other orders of the 4 GiB size-sweep configuration)
     sweep = {}
     if not args.no_sweep:
-        for n in SWEEP_NS:
-            batch = (4 << 30) // (16 * n * n)
-            A, eig, flag, work = alloc(n, batch)
-            call(n, batch, A, eig, flag, work)
-            torch.cuda.synchronize()
-            e0 = torch.cuda.Event(enable_timing=True)
-            e1 = torch.cuda.Event(enable_timing=True)
-            reps = 2
-            e0.record(stream)
-            for _ in range(reps):
-                call(n, batch, A, eig, flag, work)
-            e1.record(stream)
-            torch.cuda.synchronize()
-            ms = e0.elapsed_time(e1) / reps
-            rate = batch / (ms * 1e-3)
-            sweep[str(n)] = {"batch": batch, "matrices_per_s": rate,
-                             "fp64_frac": flops_per_matrix(n) * rate / peak,
-                             "flagged": int((flag != 0).sum().item())}
-            del A, eig, flag, work
-            torch.cuda.empty_cache()
-        sweep[str(N)] = {"batch": BATCH, "matrices_per_s": value / ws, "fp64_frac": achieved / peak,
-                         "flagged": flagged}
+        for cls in ("gaussian", "vdv", "companion"):
+            res = {}
+            for n in SWEEP_NS + (N,):
+                if cls == "gaussian" and n == N:
+                    res[str(n)] = {"batch": BATCH, "matrices_per_s": value / ws, "fp64_frac": achieved / peak,
+                                   "flagged": flagged, "parity": parity}
+                    continue
+                batch = (4 << 30) // (16 * n * n)
+                A, eig, flag, work = alloc(n, batch, gen=cls, seed=SEED + 17 * n)
+                ms = time_ms(lambda: call(n, batch, A, eig, flag, work), 2, stream)
+                rate = batch / (ms * 1e-3)
+                res[str(n)] = {"batch": batch, "matrices_per_s": rate,
+                               "fp64_frac": flops_per_matrix(n) * rate / peak,
+                               "flagged": int((flag != 0).sum().item())}
+                if rank == 0 and not args.no_check:
+                    res[str(n)]["parity"] = spot_check(A, eig, flag, 128)
+                del A, eig, flag, work
+                torch.cuda.empty_cache()
+            sweep[cls] = res
 
     config1 = None
     if not args.no_sweep:

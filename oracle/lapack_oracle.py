@@ -32,6 +32,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libcpu_zgeev.so")
 SRC = os.path.join(HERE, "cpu_zgeev.c")
+REF_SRC = os.path.join(HERE, "ref_algorithm.c")
 
 TOL_REL_FRO = 1e-11
 COND_MAX = 1e3
@@ -52,11 +53,14 @@ def find_lapack() -> str:
 
 def build(force: bool = False) -> str:
     """Compiles the C harness with gcc (plain C, no vendored sources)."""
-    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= os.path.getmtime(SRC):
+    newest = max(os.path.getmtime(SRC), os.path.getmtime(REF_SRC))
+    if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= newest:
         return LIB_PATH
     os.makedirs(BUILD_DIR, exist_ok=True)
     tmp = LIB_PATH + ".tmp"
-    cmd = ["gcc", "-O2", "-std=c11", "-shared", "-fPIC", "-o", tmp, SRC, "-ldl", "-lpthread"]
+    # -ffp-contract=off: the restatement rounds each operation as written.
+    cmd = ["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-shared", "-fPIC", "-o", tmp, SRC, REF_SRC, "-ldl",
+           "-lpthread", "-lm"]
     subprocess.run(cmd, check=True, capture_output=True)
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
@@ -73,6 +77,8 @@ def _load():
         lib.cpu_zgeevx_batched.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                            ctypes.POINTER(ctypes.c_double)]
+        lib.ref_zgeev_batched.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_void_p]
         st = lib.cpu_zgeev_open(find_lapack().encode())
         if st != 0:
             raise RuntimeError(f"cannot open LAPACK ({st})")
@@ -121,6 +127,20 @@ def zgeevx_rconde(A: np.ndarray, threads: int | None = None):
     lib.cpu_zgeevx_batched(n, b, A.ctypes.data, w.ctypes.data, rc.ctypes.data, info.ctypes.data,
                            threads or default_threads(), ctypes.byref(sec))
     return w, rc, info
+
+
+def reference_algorithm(A: np.ndarray):
+    """The reference's own GPU algorithm restated serially in C (oracle/ref_algorithm.c).
+
+    Returns ``(w[batch, n], flag[batch])``; flag 1 means its n^4 sweep cap was hit.
+    """
+    lib = _load()
+    A = _as_batch(A)
+    b, n, _ = A.shape
+    w = np.empty((b, n), np.complex128)
+    flag = np.empty(b, np.int32)
+    lib.ref_zgeev_batched(n, b, A.ctypes.data, w.ctypes.data, flag.ctypes.data)
+    return w, flag
 
 
 def matched_abs_errors(w_test: np.ndarray, w_ref: np.ndarray) -> np.ndarray:

@@ -127,3 +127,14 @@ def test_lane_configs_agree(cuda):
         outs.append(w.cpu().numpy())
     for w in outs[1:]:
         assert lo.matched_abs_errors(w, outs[0]).max() < 1e-11 * 33
+
+
+def test_purely_imaginary_subdiagonal(cuda):
+    """A case the reference's real-part-only deflation test gets wrong (see tests/test_oracle.py)."""
+    import torch
+
+    H = np.array([[1, 2, 3], [2j, 4, 5], [0, 3j, 6]], np.complex128)
+    A = np.stack([H, H.T.copy()])
+    w, f = api.zgeev_batched(torch.from_numpy(A).cuda())
+    rep = lo.parity_report(A, w.cpu().numpy(), f.cpu().numpy())
+    assert rep["flag_mismatch"] == 0 and rep["max_rel_err"] <= lo.TOL_REL_FRO

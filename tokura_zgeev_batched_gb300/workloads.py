@@ -108,13 +108,14 @@ def torch_gaussian(batch: int, n: int, seed: int = SEED, device: str = "cuda"):
     return torch.complex(re, im)
 
 
-def torch_vdv(batch: int, n: int, seed: int = SEED, device: str = "cuda", chunk: int = 8192):
+def torch_vdv(batch: int, n: int, seed: int = SEED, device: str = "cuda", chunk: int = 0):
     import torch
 
     g = torch.Generator(device=device)
     g.manual_seed(seed)
     out = torch.empty(batch, n, n, dtype=torch.complex128, device=device)
     eye = torch.eye(n, dtype=torch.complex128, device=device)
+    chunk = chunk or max(8192, (1 << 25) // (n * n))
     for s in range(0, batch, chunk):
         b = min(chunk, batch - s)
         r = torch.sqrt(torch.rand(b, n, generator=g, device=device, dtype=torch.float64))
