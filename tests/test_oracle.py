@@ -91,7 +91,9 @@ def test_condition_numbers_match_eigenvector_formula():
 
 # ---- CPU restatement of the reference's own algorithm (oracle/ref_algorithm.c)
 
-QUIRK_PURELY_IMAGINARY_SUBDIAGONAL = np.array([[1, 2, 3], [2j, 4, 5], [0, 3j, 6]], np.complex128)
+# Buffers are read column-major, so the row-major array holds H^T for the Hessenberg matrix
+# H = [[1, 2, 3], [2i, 4, 5], [0, 3i, 6]].
+QUIRK_PURELY_IMAGINARY_SUBDIAGONAL = np.array([[1, 2, 3], [2j, 4, 5], [0, 3j, 6]], np.complex128).T.copy()
 
 
 def test_reference_algorithm_matches_published_error_level():
