@@ -119,6 +119,20 @@ TOKURA_API size_t tokura_get_zgeev_ragged_backward_workspacesize(int batch_count
 /* Lanes per matrix of the ragged solver (1, 2, 4; 0 = choose from batch_count). */
 TOKURA_API int tokuraSetRaggedLanes(tokurablas_t* handle, int lanes_per_matrix);
 
+/* Host-buffer variant of tokura_zgeev_batched_gpu: A, eigenvalues and flag are
+ * HOST pointers (layouts as the device call). The batch is cut into chunks of
+ * chunk_matrices (0 = automatic) issued round-robin on the handle's own
+ * streams, so host-device copies overlap the solves; returns when the results
+ * are in host memory. Replaces the reference's multi-stream example driver
+ * (stream_test_with_MKL/main.cu:236-288). Host memory should be pinned for the
+ * copies to overlap. Device buffers are cached in the handle (freed by
+ * tokuraDestroy); host-buffer calls on one handle are serialized.
+ * Returns 0; -1 NULL handle, -2 bad n, -3 A NULL, -4 eigenvalues NULL,
+ * -6 batch_count <= 0, -7 flag NULL, -8 chunk_matrices < 0; 2 device
+ * allocation failure, 1 CUDA failure. */
+TOKURA_API int tokura_zgeev_batched_host(tokurablas_t* handle, int n, int batch_count, const cuDoubleComplex* A,
+                                         cuDoubleComplex* eigenvalues, char* flag, int chunk_matrices);
+
 /* Same computation and outputs as tokura_zgeev_batched_gpu, but it allocates
  * nothing and takes no workspace: it has no counterpart in the reference.
  * It is for callers that cannot allocate device memory when they need the

@@ -56,6 +56,8 @@ _SIGNATURES = {
     "tokuraAutotuneRagged": (ctypes.c_int,
                              [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
     "tokuraSaveTuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
+    "tokura_zgeev_batched_host": (
+        ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 3 + [ctypes.c_int]),
     "tokura_zgeev_backward_gpu": (
         ctypes.c_int,
         [ctypes.c_void_p, ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 7,
@@ -364,3 +366,39 @@ def zgeev_backward(A, eigenvalues, grad_eigenvalues, handle: Handle | None = Non
     if st != 0:
         raise RuntimeError(f"tokura_zgeev_backward_gpu returned {st}")
     return gA.reshape(A.shape), flag
+
+
+def tokura_zgeev_batched_host(handle, n: int, batch_count: int, A: int, eigenvalues: int, flag: int,
+                              chunk_matrices: int = 0) -> int:
+    """Host-buffer entry point (host addresses as integers); blocks until the results are on the host."""
+    return int(lib().tokura_zgeev_batched_host(_ptr(handle), int(n), int(batch_count), A, eigenvalues, flag,
+                                               int(chunk_matrices)))
+
+
+def zgeev_batched_host(A, handle: Handle | None = None, chunk_matrices: int = 0):
+    """Eigenvalues of host-resident matrices (numpy complex128 ``[..., n, n]`` or a CPU torch tensor).
+
+    Pinned (page-locked) torch tensors let the copies overlap the solves.
+    Returns numpy ``(eigenvalues[..., n], flag[...])``.
+    """
+    import numpy as np
+
+    if hasattr(A, "numpy"):
+        arr = A.contiguous()
+        ptr = arr.data_ptr()
+        shape = tuple(arr.shape)
+        keep = arr
+    else:
+        keep = np.ascontiguousarray(A, dtype=np.complex128)
+        ptr = keep.ctypes.data
+        shape = keep.shape
+    n = shape[-1]
+    batch = int(np.prod(shape[:-2])) if len(shape) > 2 else 1
+    eig = np.empty((batch, n), np.complex128)
+    flag = np.empty(batch, np.int8)
+    h = handle if handle is not None else default_handle()
+    st = tokura_zgeev_batched_host(h, n, batch, ptr, eig.ctypes.data, flag.ctypes.data, chunk_matrices)
+    del keep
+    if st != 0:
+        raise RuntimeError(f"tokura_zgeev_batched_host returned {st}")
+    return eig.reshape(*shape[:-2], n), flag.reshape(shape[:-2])

@@ -34,6 +34,7 @@ SOURCES = [
     "zgeev_backward.cu",
     "tokura_capi.cpp",
     "compat_cxx.cpp",
+    "tokura_host_pipeline.cpp",
 ]
 
 

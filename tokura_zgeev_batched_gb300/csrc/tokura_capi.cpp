@@ -33,6 +33,13 @@ extern "C" int tokuraCreate(tokurablas_t** handle) {
 }
 
 extern "C" int tokuraDestroy(tokurablas_t* handle) {
+  if (handle != nullptr) {
+    int prev = 0;
+    const bool switch_dev = cudaGetDevice(&prev) == cudaSuccess && prev != handle->device;
+    if (switch_dev) cudaSetDevice(handle->device);
+    handle->pipe.release();
+    if (switch_dev) cudaSetDevice(prev);
+  }
   delete handle;
   return 0;
 }

@@ -1,7 +1,26 @@
 // Contents of the opaque tokurablas_t handle and the launch-shape policy.
 #pragma once
 
+#include <mutex>
+
 #include "zgeev_internal.h"
+
+namespace tzg {
+
+// Device buffers and streams of the host-buffer entry point, cached per handle.
+struct HostPipeline {
+  static constexpr int kStreams = 4;
+  void* d_a[kStreams] = {};
+  void* d_eig[kStreams] = {};
+  void* d_work[kStreams] = {};
+  char* d_flag[kStreams] = {};
+  cudaStream_t stream[kStreams] = {};
+  cudaEvent_t done = nullptr;
+  size_t cap_a = 0, cap_eig = 0, cap_work = 0, cap_flag = 0;
+  void release();
+};
+
+}  // namespace tzg
 
 struct tokurablas_t {
   int device = 0;
@@ -9,7 +28,9 @@ struct tokurablas_t {
   int itmax_override = 0;  // >0 replaces the per-eigenvalue sweep cap 30*max(10,n)
   // Tuned plain-kernel shape per n (index 1..64); lanes == 0 means "heuristic".
   tzg::PlainConfig plain[65] = {};
-  int ragged_lanes = 0;  // lanes per matrix of the ragged solvers; 0 = chosen per size bin on the device
+  int ragged_lanes = 0;  // lanes per matrix of the ragged solvers; 0 = chosen per launch
+  tzg::HostPipeline pipe;  // host-buffer entry point state (guarded by pipe_mutex)
+  std::mutex pipe_mutex;
 };
 
 namespace tzg {

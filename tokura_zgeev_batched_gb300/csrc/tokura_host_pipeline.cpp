@@ -1,0 +1,115 @@
+// Host-buffer entry point: eigenvalues of matrices that live in host memory.
+//
+// Replaces the reference's multi-stream example driver
+// (stream_test_with_MKL/main.cu:236-288: 8 streams x 8192-matrix chunks of
+// H2D copy, tokura_zgeev_batched_gpu, D2H copy) with a library call. The
+// batch is cut into chunks that are issued round-robin on the handle's own
+// streams, so the copies of one chunk overlap the solves of others and
+// several chunk kernels run side by side on the GPU. Device buffers are
+// cached in the handle (grown on demand, freed by tokuraDestroy); a mutex in
+// the handle serializes host-buffer calls on the same handle. Host memory
+// should be pinned (cudaHostAlloc / cudaHostRegister) for the copies to
+// overlap; pageable memory works but the driver then stages each copy.
+#include <mutex>
+
+#include "../../include/tokura_blas_ext.h"
+#include "tokura_handle.h"
+#include "zgeev_internal.h"
+
+namespace tzg {
+
+void HostPipeline::release() {
+  for (int s = 0; s < kStreams; ++s) {
+    if (d_a[s]) cudaFree(d_a[s]);
+    if (d_eig[s]) cudaFree(d_eig[s]);
+    if (d_work[s]) cudaFree(d_work[s]);
+    if (d_flag[s]) cudaFree(d_flag[s]);
+    if (stream[s]) cudaStreamDestroy(stream[s]);
+    d_a[s] = d_eig[s] = d_work[s] = nullptr;
+    d_flag[s] = nullptr;
+    stream[s] = nullptr;
+  }
+  if (done) cudaEventDestroy(done);
+  done = nullptr;
+  cap_a = cap_eig = cap_work = cap_flag = 0;
+}
+
+static cudaError_t grow(void** p, size_t* cap, size_t need) {
+  if (need <= *cap) return cudaSuccess;
+  if (*p) cudaFree(*p);
+  *p = nullptr;
+  *cap = 0;
+  cudaError_t err = cudaMalloc(p, need);
+  if (err == cudaSuccess) *cap = need;
+  return err;
+}
+
+static cudaError_t ensure(HostPipeline& P, int n, int chunk) {
+  cudaError_t err;
+  for (int s = 0; s < HostPipeline::kStreams; ++s) {
+    if (!P.stream[s] && (err = cudaStreamCreateWithFlags(&P.stream[s], cudaStreamNonBlocking)) != cudaSuccess)
+      return err;
+  }
+  if (!P.done && (err = cudaEventCreateWithFlags(&P.done, cudaEventDisableTiming)) != cudaSuccess) return err;
+  const size_t a = sizeof(double2) * (size_t)n * n * chunk;
+  const size_t e = sizeof(double2) * (size_t)n * chunk;
+  for (int s = 0; s < HostPipeline::kStreams; ++s) {
+    size_t ca = P.cap_a, ce = P.cap_eig, cw = P.cap_work, cf = P.cap_flag;
+    if ((err = grow(&P.d_a[s], &ca, a)) != cudaSuccess) return err;
+    if ((err = grow(&P.d_eig[s], &ce, e)) != cudaSuccess) return err;
+    if ((err = grow(&P.d_work[s], &cw, a)) != cudaSuccess) return err;
+    if ((err = grow(reinterpret_cast<void**>(&P.d_flag[s]), &cf, (size_t)chunk)) != cudaSuccess) return err;
+  }
+  if (a > P.cap_a) P.cap_a = a;
+  if (e > P.cap_eig) P.cap_eig = e;
+  if (a > P.cap_work) P.cap_work = a;
+  if ((size_t)chunk > P.cap_flag) P.cap_flag = chunk;
+  return cudaSuccess;
+}
+
+}  // namespace tzg
+
+extern "C" TOKURA_API int tokura_zgeev_batched_host(tokurablas_t* handle, int n, int batch_count,
+                                                    const cuDoubleComplex* A, cuDoubleComplex* eigenvalues,
+                                                    char* flag, int chunk_matrices) {
+  if (handle == nullptr) return -1;
+  if (!(n > 0 && n <= TOKURA_ZGEEV_BATCHED_MAX_MATRIX_SIZE)) return -2;
+  if (A == nullptr) return -3;
+  if (eigenvalues == nullptr) return -4;
+  if (!(batch_count > 0)) return -6;
+  if (flag == nullptr) return -7;
+  if (chunk_matrices < 0) return -8;
+  using tzg::HostPipeline;
+  // Default chunk: one round over the streams, but at least 1024 matrices per chunk.
+  int chunk = chunk_matrices;
+  if (chunk == 0) {
+    chunk = (batch_count + HostPipeline::kStreams - 1) / HostPipeline::kStreams;
+    if (chunk < 1024) chunk = 1024;
+  }
+  if (chunk > batch_count) chunk = batch_count;
+  std::lock_guard<std::mutex> lock(handle->pipe_mutex);
+  HostPipeline& P = handle->pipe;
+  if (tzg::ensure(P, n, chunk) != cudaSuccess) return 2;
+  const int itmax = handle->itmax_override > 0 ? handle->itmax_override : tzg::default_itmax(n);
+  const size_t nn = (size_t)n * n;
+  int k = 0;
+  for (long long first = 0; first < batch_count; first += chunk, ++k) {
+    const int s = k % HostPipeline::kStreams;
+    const int m = (int)((batch_count - first) < chunk ? (batch_count - first) : chunk);
+    cudaStream_t st = P.stream[s];
+    if (cudaMemcpyAsync(P.d_a[s], A + first * nn, sizeof(double2) * nn * m, cudaMemcpyHostToDevice, st) !=
+        cudaSuccess)
+      return 1;
+    const tzg::PlainConfig cfg = tzg::plain_config_for(handle, n, batch_count);  // chunks run side by side
+    if (tzg::launch_plain(cfg, n, m, static_cast<const double2*>(P.d_a[s]), static_cast<double2*>(P.d_eig[s]),
+                          static_cast<double2*>(P.d_work[s]), P.d_flag[s], itmax, st) != cudaSuccess)
+      return 1;
+    if (cudaMemcpyAsync(eigenvalues + first * n, P.d_eig[s], sizeof(double2) * (size_t)n * m,
+                        cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaMemcpyAsync(flag + first, P.d_flag[s], (size_t)m, cudaMemcpyDeviceToHost, st) != cudaSuccess)
+      return 1;
+  }
+  for (int s = 0; s < HostPipeline::kStreams; ++s)
+    if (cudaStreamSynchronize(P.stream[s]) != cudaSuccess) return 1;
+  return 0;
+}
