@@ -21,7 +21,7 @@ extern "C" {
  * do not race it with compute calls on the same handle. */
 TOKURA_API int tokuraSetSweepCap(tokurablas_t* handle, int cap);
 
-/* Launch shape of the plain kernel for order n: lanes per matrix (1, 2 or 4;
+/* Launch shape of the plain kernel for order n: lanes per matrix (1, 2, 4, 8;
  * 0 = choose from the batch size) and threads per block (32..256, multiple
  * of 32; 0 = 128). Replaces the reference's compile-time tables
  * (include/tokura_zhseqr_parameters.h, tokura_zgeev_batched.cu:13-60).
@@ -35,15 +35,15 @@ TOKURA_API int tokuraGetPlainConfig(const tokurablas_t* handle, int n, int batch
 /* Autotuner (replaces the reference's build-time tuner,
  * src/TOKURA_ZHSEQR_BATCHED_GEHRD_TUNING_main.cu:89-227, and its generated
  * tables). For each order n in [n_min, n_max], times every plain-kernel shape
- * (lanes per matrix 1/2/4 x threads per block 64/128/256) on batch_count
+ * (lanes per matrix 1/2/4/8 x threads per block 64/128/256) on batch_count
  * seeded synthetic complex Gaussian matrices and stores the fastest in the
  * handle. Allocates its own scratch (cudaMalloc), synchronizes `stream`.
  * Returns 0; -1 NULL handle, -2 bad range, -6 batch_count <= 0,
  * 2 allocation failure, 1 CUDA failure. */
 TOKURA_API int tokuraAutotune(tokurablas_t* handle, int n_min, int n_max, int batch_count, cudaStream_t stream);
 
-/* Same for the ragged solver (lanes per matrix) on batch_count matrices with
- * orders uniform in [n_min, n_max]. */
+/* Same for the ragged solvers (lanes per matrix, 0 = automatic, 1, 2, 4, 8) on
+ * batch_count matrices with orders uniform in [n_min, n_max]. */
 TOKURA_API int tokuraAutotuneRagged(tokurablas_t* handle, int batch_count, int n_min, int n_max,
                                     cudaStream_t stream);
 
@@ -116,7 +116,21 @@ TOKURA_API int tokura_zgeev_ragged_backward_gpu(tokurablas_t* handle, int batch_
                                                 void* work, char* flag, cudaStream_t stream);
 TOKURA_API size_t tokura_get_zgeev_ragged_backward_workspacesize(int batch_count, long long total_elements);
 
-/* Lanes per matrix of the ragged solver (1, 2, 4; 0 = choose from batch_count). */
+/* Eigenvalues and eigenvectors (ZGEEV with JOBVL/JOBVR = 'V'; the reference
+ * computes eigenvalues only, README.md:63). VR[:, i] / VL[:, i] (column-major
+ * n x n per matrix, matrices one after another) are the right / left
+ * eigenvectors of eigenvalues[i] (A VR = VR diag(w), VL^H A = diag(w) VL^H),
+ * each with unit 2-norm and its largest-modulus component real and positive,
+ * as LAPACK zgeev returns them. VL or VR may be NULL. flag: 0 converged,
+ * 1 QR cap hit, 2 non-finite input. work:
+ * tokura_get_zgeev_vectors_workspacesize(n, batch_count) bytes (48*n*n*batch
+ * + 16*n*batch). Return codes as tokura_zgeev_batched_gpu. */
+TOKURA_API int tokura_zgeev_vectors_batched_gpu(tokurablas_t* handle, int n, int batch_count, const cuDoubleComplex* A,
+                                                cuDoubleComplex* eigenvalues, cuDoubleComplex* VL,
+                                                cuDoubleComplex* VR, void* work, char* flag, cudaStream_t stream);
+TOKURA_API size_t tokura_get_zgeev_vectors_workspacesize(int n, int batch_count);
+
+/* Lanes per matrix of the ragged solvers (1, 2, 4, 8; 0 = chosen per launch). */
 TOKURA_API int tokuraSetRaggedLanes(tokurablas_t* handle, int lanes_per_matrix);
 
 /* Host-buffer variant of tokura_zgeev_batched_gpu: A, eigenvalues and flag are

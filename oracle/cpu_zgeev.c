@@ -50,11 +50,13 @@ int cpu_zgeev_open(const char* path) {
 }
 
 typedef struct {
-  int n, batch, mode;
-  const double* A; /* batch * n * n complex (interleaved re, im), column-major */
-  double* w;       /* batch * n complex */
-  double* rconde;  /* batch * n (mode 1) */
-  int* info;       /* batch */
+  int n, batch, mode; /* mode 0: eigenvalues, 1: + RCONDE, 2: + left/right eigenvectors */
+  const double* A;    /* batch * n * n complex (interleaved re, im), column-major */
+  double* w;          /* batch * n complex */
+  double* rconde;     /* batch * n (mode 1) */
+  double* vl;         /* batch * n * n complex (mode 2) */
+  double* vr;         /* batch * n * n complex (mode 2) */
+  int* info;          /* batch */
   atomic_long next;
 } job_t;
 
@@ -79,6 +81,9 @@ static void* worker(void* arg) {
       memcpy(a, J->A + (size_t)k * nn2, sizeof(double) * nn2);
       if (J->mode == 0) {
         J->info[k] = g_zgeev(LAPACK_COL_MAJOR_, 'N', 'N', n, a, n, J->w + (size_t)k * n * 2, NULL, 1, NULL, 1);
+      } else if (J->mode == 2) {
+        J->info[k] = g_zgeev(LAPACK_COL_MAJOR_, 'V', 'V', n, a, n, J->w + (size_t)k * n * 2, J->vl + (size_t)k * nn2, n,
+                             J->vr + (size_t)k * nn2, n);
       } else {
         int ilo, ihi;
         double abnrm;
@@ -109,7 +114,15 @@ static int run(job_t* J, int nthreads, double* seconds) {
 /* Eigenvalues of `batch` matrices with zgeev('N','N'); info[k] is LAPACK's INFO. */
 int cpu_zgeev_batched(int n, int batch, const double* A, double* w, int* info, int nthreads, double* seconds) {
   job_t J;
-  J.n = n; J.batch = batch; J.mode = 0; J.A = A; J.w = w; J.rconde = NULL; J.info = info;
+  J.n = n; J.batch = batch; J.mode = 0; J.A = A; J.w = w; J.rconde = NULL; J.vl = NULL; J.vr = NULL; J.info = info;
+  return run(&J, nthreads, seconds);
+}
+
+/* Eigenvalues and left/right eigenvectors with zgeev('V','V'). */
+int cpu_zgeev_vectors_batched(int n, int batch, const double* A, double* w, double* vl, double* vr, int* info,
+                              int nthreads, double* seconds) {
+  job_t J;
+  J.n = n; J.batch = batch; J.mode = 2; J.A = A; J.w = w; J.rconde = NULL; J.vl = vl; J.vr = vr; J.info = info;
   return run(&J, nthreads, seconds);
 }
 
@@ -117,6 +130,6 @@ int cpu_zgeev_batched(int n, int batch, const double* A, double* w, int* info, i
 int cpu_zgeevx_batched(int n, int batch, const double* A, double* w, double* rconde, int* info, int nthreads,
                        double* seconds) {
   job_t J;
-  J.n = n; J.batch = batch; J.mode = 1; J.A = A; J.w = w; J.rconde = rconde; J.info = info;
+  J.n = n; J.batch = batch; J.mode = 1; J.A = A; J.w = w; J.rconde = rconde; J.vl = NULL; J.vr = NULL; J.info = info;
   return run(&J, nthreads, seconds);
 }

@@ -77,6 +77,8 @@ def _load():
         lib.cpu_zgeevx_batched.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                            ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
                                            ctypes.POINTER(ctypes.c_double)]
+        lib.cpu_zgeev_vectors_batched.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 5 + [
+            ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
         lib.ref_zgeev_batched.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.c_void_p]
         st = lib.cpu_zgeev_open(find_lapack().encode())
@@ -113,6 +115,23 @@ def zgeev(A: np.ndarray, threads: int | None = None):
     lib.cpu_zgeev_batched(n, b, A.ctypes.data, w.ctypes.data, info.ctypes.data, threads or default_threads(),
                           ctypes.byref(sec))
     return w, info, sec.value
+
+
+def zgeev_vectors(A: np.ndarray, threads: int | None = None):
+    """zgeev('V','V'): ``(w, VL, VR, info)``; VL/VR ``[batch, n, n]`` with column i (``VR[k][:, i]``)
+    the eigenvector of ``w[k, i]`` for the column-major reading of ``A[k]``."""
+    lib = _load()
+    A = _as_batch(A)
+    b, n, _ = A.shape
+    w = np.empty((b, n), np.complex128)
+    vl = np.empty((b, n, n), np.complex128)
+    vr = np.empty((b, n, n), np.complex128)
+    info = np.empty(b, np.int32)
+    sec = ctypes.c_double()
+    lib.cpu_zgeev_vectors_batched(n, b, A.ctypes.data, w.ctypes.data, vl.ctypes.data, vr.ctypes.data,
+                                  info.ctypes.data, threads or default_threads(), ctypes.byref(sec))
+    # Buffers are column-major: element (r, c) of matrix k sits at [k, c, r] of the array.
+    return w, vl.transpose(0, 2, 1), vr.transpose(0, 2, 1), info
 
 
 def zgeevx_rconde(A: np.ndarray, threads: int | None = None):

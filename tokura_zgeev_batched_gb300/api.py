@@ -56,6 +56,9 @@ _SIGNATURES = {
     "tokuraAutotuneRagged": (ctypes.c_int,
                              [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
     "tokuraSaveTuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
+    "tokura_zgeev_vectors_batched_gpu": (
+        ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 7),
+    "tokura_get_zgeev_vectors_workspacesize": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int]),
     "tokura_zgeev_batched_host": (
         ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 3 + [ctypes.c_int]),
     "tokura_zgeev_backward_gpu": (
@@ -402,3 +405,39 @@ def zgeev_batched_host(A, handle: Handle | None = None, chunk_matrices: int = 0)
     if st != 0:
         raise RuntimeError(f"tokura_zgeev_batched_host returned {st}")
     return eig.reshape(*shape[:-2], n), flag.reshape(shape[:-2])
+
+
+def zgeev_vectors(A, left: bool = True, right: bool = True, handle: Handle | None = None, stream=None):
+    """Eigenvalues and eigenvectors of complex128 CUDA matrices ``A[..., n, n]`` (ZGEEV with 'V').
+
+    The matrices are taken as stored by torch (row-major). Returns
+    ``(w[..., n], VL, VR, flag)`` with ``VR[..., :, i]`` the right eigenvector of
+    ``w[..., i]`` (``A @ VR = VR @ diag(w)``) and ``VL[..., :, i]`` the left one
+    (``VL^H @ A = diag(w) @ VL^H``), each unit-norm with its largest component
+    real; VL / VR are None when not requested.
+    """
+    import torch
+
+    n = A.shape[-1]
+    batch_shape = A.shape[:-2]
+    # The library reads column-major buffers: pass A^T (row-major A read as column-major is A^T).
+    At = A.reshape(-1, n, n).transpose(-1, -2).contiguous()
+    batch = At.shape[0]
+    w = torch.empty(batch, n, dtype=torch.complex128, device=A.device)
+    flag = torch.empty(batch, dtype=torch.int8, device=A.device)
+    VLc = torch.empty(batch, n, n, dtype=torch.complex128, device=A.device) if left else None
+    VRc = torch.empty(batch, n, n, dtype=torch.complex128, device=A.device) if right else None
+    work = torch.empty(int(lib().tokura_get_zgeev_vectors_workspacesize(n, batch)), dtype=torch.uint8,
+                       device=A.device)
+    s = stream if stream is not None else torch.cuda.current_stream(A.device)
+    h = handle if handle is not None else default_handle()
+    st = int(lib().tokura_zgeev_vectors_batched_gpu(_ptr(h), n, batch, At.data_ptr(), w.data_ptr(),
+                                                    VLc.data_ptr() if left else None,
+                                                    VRc.data_ptr() if right else None, work.data_ptr(),
+                                                    flag.data_ptr(), s.cuda_stream))
+    if st != 0:
+        raise RuntimeError(f"tokura_zgeev_vectors_batched_gpu returned {st}")
+    # Column-major results read back row-major are transposed: undo.
+    VL = VLc.transpose(-1, -2).reshape(*batch_shape, n, n) if left else None
+    VR = VRc.transpose(-1, -2).reshape(*batch_shape, n, n) if right else None
+    return w.reshape(*batch_shape, n), VL, VR, flag.reshape(batch_shape)

@@ -32,6 +32,7 @@ SOURCES = [
     "zgeev_ragged.cu",
     "tokura_tuner.cu",
     "zgeev_backward.cu",
+    "zgeev_vectors.cu",
     "tokura_capi.cpp",
     "compat_cxx.cpp",
     "tokura_host_pipeline.cpp",

@@ -188,3 +188,28 @@ extern "C" int tokura_zgeev_ragged_backward_gpu(tokurablas_t* handle, int batch_
       handle->itmax_override, stream);
   return err == cudaSuccess ? 0 : 1;
 }
+
+extern "C" size_t tokura_get_zgeev_vectors_workspacesize(int n, int batch_count) {
+  if (!(0 < n && n <= TOKURA_ZGEEV_BATCHED_MAX_MATRIX_SIZE)) return (size_t)-1;
+  if (!(0 < batch_count)) return (size_t)-2;
+  return tzg::backward_workspace_bytes(n, batch_count);
+}
+
+extern "C" int tokura_zgeev_vectors_batched_gpu(tokurablas_t* handle, int n, int batch_count,
+                                                const cuDoubleComplex* A, cuDoubleComplex* eigenvalues,
+                                                cuDoubleComplex* VL, cuDoubleComplex* VR, void* work, char* flag,
+                                                cudaStream_t stream) {
+  if (handle == nullptr) return -1;
+  if (!(n > 0 && n <= TOKURA_ZGEEV_BATCHED_MAX_MATRIX_SIZE)) return -2;
+  if (A == nullptr) return -3;
+  if (eigenvalues == nullptr) return -4;
+  if (work == nullptr) return -5;
+  if (!(batch_count > 0)) return -6;
+  if (flag == nullptr) return -7;
+  const int lanes = tzg::plain_config_for(handle, n, batch_count).lanes;
+  const int itmax = handle->itmax_override > 0 ? handle->itmax_override : tzg::default_itmax(n);
+  const cudaError_t err = tzg::launch_vectors(
+      lanes, n, batch_count, reinterpret_cast<const double2*>(A), reinterpret_cast<double2*>(eigenvalues),
+      reinterpret_cast<double2*>(VL), reinterpret_cast<double2*>(VR), static_cast<double2*>(work), flag, itmax, stream);
+  return err == cudaSuccess ? 0 : 1;
+}

@@ -91,12 +91,15 @@ __device__ __forceinline__ int nearest_unused(const double2* __restrict__ lam, i
   return best;
 }
 
-// Single-shift QR to Schur form with Q accumulated. Same deflation test and
-// cap as the forward; full-width updates. Writes gbar of the matched forward
-// eigenvalue to vec[i] for every diagonal position i.
+// Single-shift QR to Schur form with Q accumulated; full-width updates.
+// Gradient mode (lam != nullptr): the forward's eigenvalues are the shifts,
+// deflation uses kGradDeflationTol, and gbar of the matched forward eigenvalue
+// is written to vec[i] for every diagonal position i. Eigenvector mode
+// (lam == nullptr): Wilkinson/ad hoc shifts and the forward's ulp-level test.
 template <int L>
 __device__ int schur_qr(const BwdViews& V, const Group<L>& G, const double2* __restrict__ lam,
                         const double2* __restrict__ gbar, double lam_scale, int itmax) {
+  const double tol = lam != nullptr ? kGradDeflationTol : kUlp;
   const MatView& T = V.T;
   const MatView& Q = V.Q;
   const int n = T.n, rs = T.rs, cs = n * rs;
@@ -108,16 +111,18 @@ __device__ int schur_qr(const BwdViews& V, const Group<L>& G, const double2* __r
     for (;;) {
       int hit = lo;
       for (int k = i - G.rank; k > lo; k -= L) {
-        if (negligible_subdiag(T, k, lo, i, smlnum, kGradDeflationTol)) {
+        if (negligible_subdiag(T, k, lo, i, smlnum, tol)) {
           hit = k;
           break;
         }
       }
       lo = G.imax(hit);
       if (lo < i) break;
-      const int kb = nearest_unused(lam, n, used, *T.at(i, i), lam_scale);
-      used |= 1ull << kb;
-      if (G.rank == 0) V.vec[i * V.vs] = gbar[kb];
+      if (lam != nullptr) {
+        const int kb = nearest_unused(lam, n, used, *T.at(i, i), lam_scale);
+        used |= 1ull << kb;
+        if (G.rank == 0) V.vec[i * V.vs] = gbar[kb];
+      }
       i -= 1;
       lo = 0;
       its = 0;
@@ -131,7 +136,7 @@ __device__ int schur_qr(const BwdViews& V, const Group<L>& G, const double2* __r
     }
     double2 sigma;
     const double2 wk = wilkinson_shift(*T.at(i - 1, i - 1), *T.at(i - 1, i), *T.at(i, i - 1), *T.at(i, i));
-    if (its == 0) {
+    if (its == 0 && lam != nullptr) {
       const double2 l = lam[nearest_unused(lam, n, used, wk, lam_scale)];
       sigma = make_double2(l.x * lam_scale, l.y * lam_scale);
       if (!(isfinite(sigma.x) && isfinite(sigma.y))) sigma = wk;

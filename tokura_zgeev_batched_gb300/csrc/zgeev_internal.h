@@ -37,4 +37,8 @@ cudaError_t launch_ragged_backward(int lanes, int sms, int batch, const int* n, 
                                    const double2* lam, const double2* gbar, double2* gA, void* work, char* flag,
                                    int itmax_override, cudaStream_t stream);
 
+// Eigenvalues with eigenvectors (workspace: backward_workspace_bytes).
+cudaError_t launch_vectors(int lanes, int n, int batch, const double2* A, double2* w, double2* VL, double2* VR,
+                           double2* work, char* flag, int itmax, cudaStream_t stream);
+
 }  // namespace tzg
