@@ -21,6 +21,15 @@ extern "C" {
  * do not race it with compute calls on the same handle. */
 TOKURA_API int tokuraSetSweepCap(tokurablas_t* handle, int cap);
 
+/* Balancing before the eigenvalue solves of later calls on this handle (plain,
+ * ragged, host-buffer and workspace-free entry points): 0 none (default, the
+ * reference's behaviour, README.md:79), 1 permutation only, 2 scaling only,
+ * 3 both (LAPACK zgeev's choice, zgebal JOB='B'). Permutation isolates
+ * eigenvalues exposed by zero rows/columns; scaling applies exact powers of
+ * two. Eigenvalues are unchanged in exact arithmetic; badly scaled matrices
+ * gain accuracy. Returns 0, -1 NULL handle, -2 bad mode. */
+TOKURA_API int tokuraSetBalancing(tokurablas_t* handle, int mode);
+
 /* Launch shape of the plain kernel for order n: lanes per matrix (1, 2, 4, 8;
  * 0 = choose from the batch size) and threads per block (32..256, multiple
  * of 32; 0 = 128). Replaces the reference's compile-time tables

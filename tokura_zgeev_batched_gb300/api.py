@@ -56,6 +56,7 @@ _SIGNATURES = {
     "tokuraAutotuneRagged": (ctypes.c_int,
                              [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
     "tokuraSaveTuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
+    "tokuraSetBalancing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "tokura_zgeev_vectors_batched_gpu": (
         ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 7),
     "tokura_get_zgeev_vectors_workspacesize": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int]),
@@ -138,6 +139,10 @@ class Handle:
 
     def load_tuning(self, path: str) -> int:
         return int(lib().tokuraLoadTuning(self.ptr, os.fsencode(path)))
+
+    def set_balancing(self, mode: int) -> int:
+        """0 none, 1 permute, 2 scale, 3 both (LAPACK zgeev's default)."""
+        return int(lib().tokuraSetBalancing(self.ptr, int(mode)))
 
     def set_ragged_lanes(self, lanes: int) -> int:
         return int(lib().tokuraSetRaggedLanes(self.ptr, int(lanes)))

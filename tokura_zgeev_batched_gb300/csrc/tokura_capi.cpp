@@ -65,7 +65,8 @@ extern "C" int tokura_zgeev_batched_gpu(tokurablas_t* handle, int n, int batch_c
   const int itmax = handle->itmax_override > 0 ? handle->itmax_override : tzg::default_itmax(n);
   const cudaError_t err = tzg::launch_plain(cfg, n, batch_count, reinterpret_cast<const double2*>(A),
                                             reinterpret_cast<double2*>(eigenvalues),
-                                            reinterpret_cast<double2*>(work), flag, itmax, cudastream);
+                                            reinterpret_cast<double2*>(work), flag, itmax, cudastream,
+                                            handle->balance_mode);
   return err == cudaSuccess ? 0 : 1;
 }
 
@@ -120,7 +121,7 @@ extern "C" int tokura_zgeev_ragged_gpu(tokurablas_t* handle, int batch_count, co
   const cudaError_t err = tzg::launch_ragged(handle->ragged_lanes, handle->sm_count, batch_count, n, offsets, eig_offsets,
                                              total_elements, reinterpret_cast<const double2*>(A),
                                              reinterpret_cast<double2*>(eigenvalues), work, flag,
-                                             handle->itmax_override, stream);
+                                             handle->itmax_override, stream, handle->balance_mode);
   return err == cudaSuccess ? 0 : 1;
 }
 
@@ -212,4 +213,11 @@ extern "C" int tokura_zgeev_vectors_batched_gpu(tokurablas_t* handle, int n, int
       lanes, n, batch_count, reinterpret_cast<const double2*>(A), reinterpret_cast<double2*>(eigenvalues),
       reinterpret_cast<double2*>(VL), reinterpret_cast<double2*>(VR), static_cast<double2*>(work), flag, itmax, stream);
   return err == cudaSuccess ? 0 : 1;
+}
+
+extern "C" int tokuraSetBalancing(tokurablas_t* handle, int mode) {
+  if (handle == nullptr) return -1;
+  if (mode < 0 || mode > 3) return -2;
+  handle->balance_mode = mode;
+  return 0;
 }

@@ -29,6 +29,7 @@ struct tokurablas_t {
   // Tuned plain-kernel shape per n (index 1..64); lanes == 0 means "heuristic".
   tzg::PlainConfig plain[65] = {};
   int ragged_lanes = 0;  // lanes per matrix of the ragged solvers; 0 = chosen per launch
+  int balance_mode = 0;  // balancing before the eigenvalue solves: 0 none (the reference's behaviour) .. 3 both
   tzg::HostPipeline pipe;  // host-buffer entry point state (guarded by pipe_mutex)
   std::mutex pipe_mutex;
 };

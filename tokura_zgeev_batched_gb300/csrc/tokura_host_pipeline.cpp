@@ -102,7 +102,8 @@ extern "C" TOKURA_API int tokura_zgeev_batched_host(tokurablas_t* handle, int n,
       return 1;
     const tzg::PlainConfig cfg = tzg::plain_config_for(handle, n, batch_count);  // chunks run side by side
     if (tzg::launch_plain(cfg, n, m, static_cast<const double2*>(P.d_a[s]), static_cast<double2*>(P.d_eig[s]),
-                          static_cast<double2*>(P.d_work[s]), P.d_flag[s], itmax, st) != cudaSuccess)
+                          static_cast<double2*>(P.d_work[s]), P.d_flag[s], itmax, st, handle->balance_mode) !=
+        cudaSuccess)
       return 1;
     if (cudaMemcpyAsync(eigenvalues + first * n, P.d_eig[s], sizeof(double2) * (size_t)n * m,
                         cudaMemcpyDeviceToHost, st) != cudaSuccess ||

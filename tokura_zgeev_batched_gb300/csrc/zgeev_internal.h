@@ -19,13 +19,13 @@ __host__ __device__ inline int default_itmax(int n) { return 30 * (n > 10 ? n : 
 // Launches the fused stage + Hessenberg + QR kernel on `stream`.
 // `work` must hold 16*n*n*batch bytes (tile-interleaved copy of A).
 cudaError_t launch_plain(const PlainConfig& cfg, int n, int batch, const double2* A, double2* eig,
-                         double2* work, char* flag, int itmax, cudaStream_t stream);
+                         double2* work, char* flag, int itmax, cudaStream_t stream, int balance = 0);
 
 // Ragged (per-matrix n) path: workspace bytes and launcher (device-side planning + persistent solve).
 size_t ragged_workspace_bytes(int batch, long long total_elements);
 cudaError_t launch_ragged(int lanes, int sms, int batch, const int* n, const long long* offsets,
                           const long long* eig_offsets, long long total_elements, const double2* A, double2* eig,
-                          void* work, char* flag, int itmax_override, cudaStream_t stream);
+                          void* work, char* flag, int itmax_override, cudaStream_t stream, int balance = 0);
 
 // Backward (Abar from A, eigenvalues and their gradients).
 size_t backward_workspace_bytes(int n, int batch);

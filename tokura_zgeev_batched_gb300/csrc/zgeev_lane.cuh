@@ -104,6 +104,119 @@ __device__ __forceinline__ void reflect_vectors(double2* const (&p)[NV], const d
   }
 }
 
+// Balancing modes (LAPACK zgebal's JOB): none, permute only, scale only, both.
+enum : int { kBalanceNone = 0, kBalancePermute = 1, kBalanceScale = 2, kBalanceBoth = 3 };
+
+// True if every entry of row (kRow) / column j inside [lo, hi], other than
+// the diagonal, is exactly zero (bit test, no FP64 work).
+template <bool kRow>
+__device__ __forceinline__ bool offdiag_zero(const MatView& M, int j, int lo, int hi) {
+  for (int k = lo; k <= hi; ++k) {
+    if (k == j) continue;
+    const double2 z = kRow ? *M.at(j, k) : *M.at(k, j);
+    const unsigned long long bits =
+        (unsigned long long)__double_as_longlong(z.x) | (unsigned long long)__double_as_longlong(z.y);
+    if ((bits << 1) != 0) return false;  // ignores the sign bit: -0.0 counts as zero
+  }
+  return true;
+}
+
+// Swaps rows and columns a and b (a similarity by a permutation).
+__device__ __forceinline__ void swap_rc(const MatView& M, int a, int b) {
+  if (a == b) return;
+  for (int k = 0; k < M.n; ++k) {
+    const double2 t = *M.at(k, a);
+    *M.at(k, a) = *M.at(k, b);
+    *M.at(k, b) = t;
+  }
+  for (int k = 0; k < M.n; ++k) {
+    const double2 t = *M.at(a, k);
+    *M.at(a, k) = *M.at(b, k);
+    *M.at(b, k) = t;
+  }
+}
+
+// Balancing before the Hessenberg reduction (the procedure of Parlett and
+// Reinsch that LAPACK's zgeev applies through zgebal; the reference does not
+// balance, README.md:79). Permutation moves rows/columns that isolate an
+// eigenvalue to the bottom/top; scaling then applies exact powers of two
+// D^{-1} A D to the remaining block [lo, hi], accepting a factor for index i
+// only when it lowers ||column i|| + ||row i|| (2-norms over [lo, hi]) by at
+// least 5 %. Eigenvalues are unchanged; the isolated ones deflate at once in
+// the QR. The permutation search (bit tests only) runs on rank 0; the norms
+// and the row/column scaling of each index are split across the group.
+template <int L>
+__device__ void balance(const MatView& M, const Group<L>& G, int mode) {
+  const int n = M.n;
+  int lo = 0, hi = n - 1;
+  if (mode & kBalancePermute) {
+    if (G.rank == 0) {
+      for (bool found = true; found && hi > lo;) {  // rows isolating an eigenvalue -> bottom
+        found = false;
+        for (int j = hi; j >= lo; --j) {
+          if (offdiag_zero<true>(M, j, lo, hi)) {
+            swap_rc(M, j, hi);
+            --hi;
+            found = true;
+            break;
+          }
+        }
+      }
+      for (bool found = true; found && hi > lo;) {  // columns isolating an eigenvalue -> top
+        found = false;
+        for (int j = lo; j <= hi; ++j) {
+          if (offdiag_zero<false>(M, j, lo, hi)) {
+            swap_rc(M, j, lo);
+            ++lo;
+            found = true;
+            break;
+          }
+        }
+      }
+    }
+    lo = G.imax(G.rank == 0 ? lo : 0);
+    hi = G.imax(G.rank == 0 ? hi : 0);
+    G.sync();
+  }
+  if (!(mode & kBalanceScale) || hi <= lo) return;
+  int total[kMaxN];  // accumulated exponent of each index, kept within +-200
+  for (int i = 0; i < n; ++i) total[i] = 0;
+  bool noconv = true;
+  for (int pass = 0; noconv && pass < 64; ++pass) {  // group-uniform control flow throughout
+    noconv = false;
+    for (int i = lo; i <= hi; ++i) {
+      double c = 0.0, r = 0.0;
+      for (int k = lo + G.rank; k <= hi; k += L) {
+        const double2 a = *M.at(k, i), b = *M.at(i, k);
+        c = fma(a.x, a.x, fma(a.y, a.y, c));
+        r = fma(b.x, b.x, fma(b.y, b.y, r));
+      }
+      c = G.sum(c);
+      r = G.sum(r);
+      if (c == 0.0 || r == 0.0) continue;
+      c = sqrt(c);
+      r = sqrt(r);
+      // Power of two f = 2^e with c*f and r/f within a factor 2 of each other.
+      int e = 0;
+      double cf = c, rf = r;
+      while (cf < rf * 0.5 && e < 60) { cf *= 2.0; rf *= 0.5; ++e; }
+      while (cf >= rf * 2.0 && e > -60) { cf *= 0.5; rf *= 2.0; --e; }
+      if (e == 0 || cf + rf >= 0.95 * (c + r)) continue;
+      if (total[i] + e > 200 || total[i] + e < -200) continue;
+      total[i] += e;
+      noconv = true;
+      const double f = pow2(e), g = pow2(-e);
+      for (int k = G.rank; k < n; k += L) {  // column i times f, row i times 1/f
+        double2* a = M.at(k, i);
+        *a = make_double2(a->x * f, a->y * f);
+        double2* b = M.at(i, k);
+        *b = make_double2(b->x * g, b->y * g);
+      }
+      G.sync();
+    }
+  }
+}
+
 // Householder reduction to upper Hessenberg form, in place. The reflector for
 // column r is P = I - tau v v^H with v[0] = 1, tau real, stored below the
 // subdiagonal of column r (v[1..]). Algorithmic FP64 work ~ (20/3) n^3 ops.
@@ -324,9 +437,11 @@ __device__ int qr_eigenvalues(const MatView& M, const Group<L>& G, double2* __re
 
 // Full solve of one matrix by its lane group: stage (with exact pre-scaling),
 // Hessenberg reduction, QR, eigenvalue write-out. Returns the flag value.
-template <int L>
+// kBalance selects the instantiation that runs balance() with balance_mode;
+// without it the balancing code is not compiled into the kernel at all.
+template <int L, bool kBalance = false>
 __device__ __forceinline__ int solve_matrix(const double2* __restrict__ src, const MatView& M, const Group<L>& G,
-                                            double2* __restrict__ ev, int itmax) {
+                                            double2* __restrict__ ev, int itmax, int balance_mode = kBalanceNone) {
   bool nonfinite, zero;
   const int shift = stage_and_scale<L>(src, M, G, nonfinite, zero);
   if (nonfinite || zero) {
@@ -334,6 +449,7 @@ __device__ __forceinline__ int solve_matrix(const double2* __restrict__ src, con
     for (int i = G.rank; i < M.n; i += L) ev[i] = make_double2(v, v);
     return nonfinite ? kNonFinite : kConverged;
   }
+  if (kBalance) balance<L>(M, G, balance_mode);
   hessenberg<L>(M, G);
   return qr_eigenvalues<L>(M, G, ev, shift, itmax);
 }

@@ -77,6 +77,7 @@ extern "C" TOKURA_API int tokura_zgeev_batched_gpu_noalloc(tokurablas_t* handle,
   const int itmax = handle->itmax_override > 0 ? handle->itmax_override : tzg::default_itmax(n);
   const cudaError_t err =
       tzg::launch_plain(cfg, n, batch_count, reinterpret_cast<const double2*>(A),
-                        reinterpret_cast<double2*>(eigenvalues), scratch, flag, itmax, cudastream);
+                        reinterpret_cast<double2*>(eigenvalues), scratch, flag, itmax, cudastream,
+                        handle->balance_mode);
   return err == cudaSuccess ? 0 : 1;
 }

@@ -11,10 +11,10 @@
 
 namespace tzg {
 
-template <int L>
+template <int L, bool kBalance>
 __global__ void __launch_bounds__(256) zgeev_plain_kernel(int n, int batch, const double2* __restrict__ A,
                                                            double2* __restrict__ eig, double2* __restrict__ work,
-                                                           char* __restrict__ flag, int itmax) {
+                                                           char* __restrict__ flag, int itmax, int balance) {
   constexpr int TW = 32 / L;
   const int lane = threadIdx.x & 31;
   const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -28,12 +28,12 @@ __global__ void __launch_bounds__(256) zgeev_plain_kernel(int n, int batch, cons
   const long long j = g0 + slot;
   MatView M{work + g0 * nn + slot, n, tw};
 
-  const int status = solve_matrix<L>(A + j * nn, M, G, eig + j * n, itmax);
+  const int status = solve_matrix<L, kBalance>(A + j * nn, M, G, eig + j * n, itmax, balance);
   if (G.rank == 0) flag[j] = (char)status;
 }
 
 cudaError_t launch_plain(const PlainConfig& cfg, int n, int batch, const double2* A, double2* eig, double2* work,
-                         char* flag, int itmax, cudaStream_t stream) {
+                         char* flag, int itmax, cudaStream_t stream, int balance) {
   const int L = cfg.lanes;
   const int tw = 32 / L;
   const long long warps = ((long long)batch + tw - 1) / tw;
@@ -42,16 +42,32 @@ cudaError_t launch_plain(const PlainConfig& cfg, int n, int batch, const double2
   if (blocks > 0x7fffffffLL || threads < 32 || threads > 256 || threads % 32 != 0) return cudaErrorInvalidValue;
   switch (L) {
     case 1:
-      zgeev_plain_kernel<1><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, eig, work, flag, itmax);
+      if (balance != 0)
+        zgeev_plain_kernel<1, true><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, eig, work, flag, itmax,
+                                                                                balance);
+      else
+        zgeev_plain_kernel<1, false><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, eig, work, flag, itmax, 0);
       break;
     case 2:
-      zgeev_plain_kernel<2><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, eig, work, flag, itmax);
+      if (balance != 0)
+        zgeev_plain_kernel<2, true><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, eig, work, flag, itmax,
+                                                                                balance);
+      else
+        zgeev_plain_kernel<2, false><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, eig, work, flag, itmax, 0);
       break;
     case 4:
-      zgeev_plain_kernel<4><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, eig, work, flag, itmax);
+      if (balance != 0)
+        zgeev_plain_kernel<4, true><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, eig, work, flag, itmax,
+                                                                                balance);
+      else
+        zgeev_plain_kernel<4, false><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, eig, work, flag, itmax, 0);
       break;
     case 8:
-      zgeev_plain_kernel<8><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, eig, work, flag, itmax);
+      if (balance != 0)
+        zgeev_plain_kernel<8, true><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, eig, work, flag, itmax,
+                                                                                balance);
+      else
+        zgeev_plain_kernel<8, false><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, eig, work, flag, itmax, 0);
       break;
     default:
       return cudaErrorInvalidValue;

@@ -200,6 +200,7 @@ struct RaggedArgs {
   char* flag;
   const int* sorted;
   int itmax_override;
+  int balance;           // forward: balancing mode
 };
 
 // Tile scheduling. Tiles are numbered in descending-work order; SM s owns
@@ -227,9 +228,10 @@ __device__ __forceinline__ int ragged_next_tile(RaggedPlan* plan, int queues, in
 }
 
 // Persistent solver with L lanes per matrix: takes tiles until all shares are
-// used up and solves (kBackward = false) or differentiates (true) each one.
+// used up and solves (kBackward = false) or differentiates (true) each one;
+// kBalance (forward only) balances each matrix first with a.balance.
 // One instantiation per lane width, so each has its own register budget.
-template <int L, bool kBackward>
+template <int L, bool kBackward, bool kBalance = false>
 __global__ void __launch_bounds__(128) zgeev_ragged_kernel(RaggedPlan* plan, RaggedArgs a, int queues) {
   constexpr int TW = 32 / L;
   const int lane = threadIdx.x & 31;
@@ -258,7 +260,8 @@ __global__ void __launch_bounds__(128) zgeev_ragged_kernel(RaggedPlan* plan, Rag
         status = backward_matrix<L>(a.A + a.offsets[j], a.lam + a.eoff[j], a.gbar + a.eoff[j],
                                     a.gA + a.offsets[j], V, G, itmax);
       } else {
-        status = solve_matrix<L>(a.A + a.offsets[j], MatView{base, nb, tw}, G, a.eig + a.eoff[j], itmax);
+        status = solve_matrix<L, kBalance>(a.A + a.offsets[j], MatView{base, nb, tw}, G, a.eig + a.eoff[j], itmax,
+                                           a.balance);
       }
       if (G.rank == 0) a.flag[j] = (char)status;
     }
@@ -273,26 +276,26 @@ static int persistent_blocks(Kernel k, int sms) {
   return sms * per_sm;
 }
 
-template <bool kBackward>
+template <bool kBackward, bool kBalance = false>
 static cudaError_t launch_ragged_kernel(int lanes, int sms, RaggedPlan* plan, const RaggedArgs& args,
                                         cudaStream_t stream) {
   const int queues = sms < 1 ? 1 : (sms > kMaxQueues ? kMaxQueues : sms);
   switch (lanes) {
     case 1:
-      zgeev_ragged_kernel<1, kBackward>
-          <<<persistent_blocks(zgeev_ragged_kernel<1, kBackward>, sms), 128, 0, stream>>>(plan, args, queues);
+      zgeev_ragged_kernel<1, kBackward, kBalance><<<persistent_blocks(zgeev_ragged_kernel<1, kBackward, kBalance>, sms),
+                                                    128, 0, stream>>>(plan, args, queues);
       break;
     case 2:
-      zgeev_ragged_kernel<2, kBackward>
-          <<<persistent_blocks(zgeev_ragged_kernel<2, kBackward>, sms), 128, 0, stream>>>(plan, args, queues);
+      zgeev_ragged_kernel<2, kBackward, kBalance><<<persistent_blocks(zgeev_ragged_kernel<2, kBackward, kBalance>, sms),
+                                                    128, 0, stream>>>(plan, args, queues);
       break;
     case 4:
-      zgeev_ragged_kernel<4, kBackward>
-          <<<persistent_blocks(zgeev_ragged_kernel<4, kBackward>, sms), 128, 0, stream>>>(plan, args, queues);
+      zgeev_ragged_kernel<4, kBackward, kBalance><<<persistent_blocks(zgeev_ragged_kernel<4, kBackward, kBalance>, sms),
+                                                    128, 0, stream>>>(plan, args, queues);
       break;
     case 8:
-      zgeev_ragged_kernel<8, kBackward>
-          <<<persistent_blocks(zgeev_ragged_kernel<8, kBackward>, sms), 128, 0, stream>>>(plan, args, queues);
+      zgeev_ragged_kernel<8, kBackward, kBalance><<<persistent_blocks(zgeev_ragged_kernel<8, kBackward, kBalance>, sms),
+                                                    128, 0, stream>>>(plan, args, queues);
       break;
     default:
       return cudaErrorInvalidValue;
@@ -342,7 +345,7 @@ static cudaError_t ragged_prepare(int lanes, int sms, int batch, const int* n, c
 
 cudaError_t launch_ragged(int lanes, int sms, int batch, const int* n, const long long* offsets,
                           const long long* eig_offsets, long long total_elements, const double2* A, double2* eig,
-                          void* work, char* flag, int itmax_override, cudaStream_t stream) {
+                          void* work, char* flag, int itmax_override, cudaStream_t stream, int balance) {
   if (lanes == 0) lanes = ragged_auto_lanes(sms, batch, total_elements);
   if (!(lanes == 1 || lanes == 2 || lanes == 4 || lanes == 8)) return cudaErrorInvalidValue;
   const RaggedLayout lay = ragged_layout(batch, total_elements);
@@ -354,7 +357,8 @@ cudaError_t launch_ragged(int lanes, int sms, int batch, const int* n, const lon
                                    stream, &plan, &sorted, &eo);
   if (err != cudaSuccess) return err;
   const RaggedArgs args{offsets, eo, A, eig, nullptr, nullptr, nullptr, stage, total_elements, flag, sorted,
-                        itmax_override};
+                        itmax_override, balance};
+  if (balance != 0) return launch_ragged_kernel<false, true>(lanes, sms, plan, args, stream);
   return launch_ragged_kernel<false>(lanes, sms, plan, args, stream);
 }
 
@@ -372,7 +376,8 @@ cudaError_t launch_ragged_backward(int lanes, int sms, int batch, const int* n, 
   cudaError_t err = ragged_prepare(lanes, sms, batch, n, offsets, eig_offsets, total_elements, lay, work, flag,
                                    stream, &plan, &sorted, &eo);
   if (err != cudaSuccess) return err;
-  const RaggedArgs args{offsets, eo, A, nullptr, lam, gbar, gA, stage, total_elements, flag, sorted, itmax_override};
+  const RaggedArgs args{offsets, eo, A, nullptr, lam, gbar, gA, stage, total_elements, flag, sorted, itmax_override,
+                        0};
   return launch_ragged_kernel<true>(lanes, sms, plan, args, stream);
 }
 
