@@ -156,6 +156,65 @@ TOKURA_API int tokuraSetRaggedLanes(tokurablas_t* handle, int lanes_per_matrix);
 TOKURA_API int tokura_zgeev_batched_host(tokurablas_t* handle, int n, int batch_count, const cuDoubleComplex* A,
                                          cuDoubleComplex* eigenvalues, char* flag, int chunk_matrices);
 
+/* Other input layouts and precisions (no reference counterpart: the
+ * reference takes contiguous n x n FP64 column-major matrices only,
+ * tokura_zgeev_batched.cu:212-285). All three use the plain solver and the
+ * workspace of tokura_get_zgeeveigenvaluesgetworspacesize(n, batch_count);
+ * results are bitwise equal to tokura_zgeev_batched_gpu on the same matrix
+ * entries. A is read only. Return codes are those of
+ * tokura_zgeev_batched_gpu plus the ones listed.
+ *
+ * Strided: matrix j is column-major at A + j*strideA with leading dimension
+ * lda (element (r,c) at A[j*strideA + r + c*lda]); its eigenvalues go to
+ * eigenvalues[j*strideW + i]. strideA may be 0 (one matrix, many copies) or
+ * smaller than lda*n (overlapping read-only views). -8 lda < n,
+ * -9 strideA < 0 or strideW < n. */
+TOKURA_API int tokura_zgeev_strided_batched_gpu(tokurablas_t* handle, int n, int batch_count, const cuDoubleComplex* A,
+                                                int lda, long long strideA, cuDoubleComplex* eigenvalues,
+                                                long long strideW, cuDoubleComplex* work, char* flag,
+                                                cudaStream_t cudastream);
+
+/* Pointer array (cuBLAS batched style): Aarray is a DEVICE array of
+ * batch_count device pointers, matrix j column-major at Aarray[j] with
+ * leading dimension lda; eigenvalues contiguous as in tokura_zgeev_batched_gpu.
+ * A NULL entry gives NaN eigenvalues and flag[j] = 3. -8 lda < n. */
+TOKURA_API int tokura_zgeev_pointer_batched_gpu(tokurablas_t* handle, int n, int batch_count,
+                                                const cuDoubleComplex* const* Aarray, int lda,
+                                                cuDoubleComplex* eigenvalues, cuDoubleComplex* work, char* flag,
+                                                cudaStream_t cudastream);
+
+/* Single-precision complex in and out (LAPACK cgeev's types), computed in
+ * FP64: entries are widened exactly on load and the eigenvalues rounded to
+ * nearest on store, so they are the FP64 eigenvalues of the given FP32
+ * matrix, correctly rounded from the FP64 result. Layout as
+ * tokura_zgeev_batched_gpu. */
+TOKURA_API int tokura_cgeev_batched_gpu(tokurablas_t* handle, int n, int batch_count, const cuComplex* A,
+                                        cuComplex* eigenvalues, cuDoubleComplex* work, char* flag,
+                                        cudaStream_t cudastream);
+
+/* Real matrices (LAPACK dgeev / sgeev with JOBVL = JOBVR = 'N'; no reference
+ * counterpart, the reference takes complex input only). Matrix j is n x n
+ * column-major at A + j*n*n; eigenvalue i of matrix j is
+ * wr[i + j*n] + i*wi[i + j*n], in LAPACK's convention: complex conjugate
+ * pairs are adjacent with the positive imaginary part first and are exact
+ * conjugates; real eigenvalues have wi exactly 0. Computed by a real
+ * Householder Hessenberg reduction and the Francis double-shift QR in FP64
+ * (about a quarter of the complex path's arithmetic). flag[j] as for
+ * tokura_zgeev_batched_gpu (balancing per tokuraSetBalancing, sweep cap per
+ * tokuraSetSweepCap). work: tokura_get_dgeev_workspacesize(n, batch_count)
+ * bytes. A is read only. Returns 0; -1 NULL handle, -2 bad n, -3 A NULL,
+ * -4 wr or wi NULL, -5 work NULL, -6 batch_count <= 0, -7 flag NULL,
+ * 1 launch failure. The sgeev variant takes FP32 A and writes FP32 wr/wi
+ * (entries widened exactly, results rounded to nearest from FP64). */
+TOKURA_API size_t tokura_get_dgeev_workspacesize(int n, int batch_count);
+TOKURA_API int tokura_dgeev_batched_gpu(tokurablas_t* handle, int n, int batch_count, const double* A, double* wr,
+                                        double* wi, double* work, char* flag, cudaStream_t cudastream);
+TOKURA_API int tokura_sgeev_batched_gpu(tokurablas_t* handle, int n, int batch_count, const float* A, float* wr,
+                                        float* wi, double* work, char* flag, cudaStream_t cudastream);
+
+/* Launch shape of the real kernel for order n (as tokuraSetPlainConfig). */
+TOKURA_API int tokuraSetRealConfig(tokurablas_t* handle, int n, int lanes_per_matrix, int threads_per_block);
+
 /* Same computation and outputs as tokura_zgeev_batched_gpu, but it allocates
  * nothing and takes no workspace: it has no counterpart in the reference.
  * It is for callers that cannot allocate device memory when they need the

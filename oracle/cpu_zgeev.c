@@ -14,7 +14,9 @@
  * call is pinned to 1, as the reference uses sequential MKL.
  *
  * Also exposes zgeevx(BALANC='N', SENSE='E') to obtain the reciprocal
- * eigenvalue condition numbers RCONDE used to filter parity checks.
+ * eigenvalue condition numbers RCONDE used to filter parity checks,
+ * zgeev('V','V') for the eigenvector path, and the real dgeev('N','N') for
+ * the real-input path (same library, same threading).
  */
 #define _GNU_SOURCE
 #include <dlfcn.h>
@@ -29,6 +31,8 @@ typedef int (*zgeev_fn)(int layout, char jobvl, char jobvr, int n, double* a, in
 typedef int (*zgeevx_fn)(int layout, char balanc, char jobvl, char jobvr, char sense, int n, double* a, int lda,
                          double* w, double* vl, int ldvl, double* vr, int ldvr, int* ilo, int* ihi, double* scale,
                          double* abnrm, double* rconde, double* rcondv);
+typedef int (*dgeev_fn)(int layout, char jobvl, char jobvr, int n, double* a, int lda, double* wr, double* wi,
+                        double* vl, int ldvl, double* vr, int ldvr);
 typedef void (*setthreads_fn)(int);
 
 enum { LAPACK_COL_MAJOR_ = 102 };
@@ -36,6 +40,7 @@ enum { LAPACK_COL_MAJOR_ = 102 };
 static void* g_lib = NULL;
 static zgeev_fn g_zgeev = NULL;
 static zgeevx_fn g_zgeevx = NULL;
+static dgeev_fn g_dgeev = NULL;
 
 /* Opens the LAPACK library; returns 0 on success. */
 int cpu_zgeev_open(const char* path) {
@@ -44,18 +49,20 @@ int cpu_zgeev_open(const char* path) {
   if (!g_lib) return -1;
   g_zgeev = (zgeev_fn)dlsym(g_lib, "scipy_LAPACKE_zgeev");
   g_zgeevx = (zgeevx_fn)dlsym(g_lib, "scipy_LAPACKE_zgeevx");
+  g_dgeev = (dgeev_fn)dlsym(g_lib, "scipy_LAPACKE_dgeev");
   setthreads_fn st = (setthreads_fn)dlsym(g_lib, "scipy_openblas_set_num_threads");
   if (st) st(1);
-  return (g_zgeev && g_zgeevx) ? 0 : -2;
+  return (g_zgeev && g_zgeevx && g_dgeev) ? 0 : -2;
 }
 
 typedef struct {
-  int n, batch, mode; /* mode 0: eigenvalues, 1: + RCONDE, 2: + left/right eigenvectors */
+  int n, batch, mode; /* mode 0: eigenvalues, 1: + RCONDE, 2: + left/right eigenvectors, 3: real dgeev */
   const double* A;    /* batch * n * n complex (interleaved re, im), column-major */
   double* w;          /* batch * n complex */
   double* rconde;     /* batch * n (mode 1) */
   double* vl;         /* batch * n * n complex (mode 2) */
   double* vr;         /* batch * n * n complex (mode 2) */
+  double* wi;         /* batch * n (mode 3; w holds wr) */
   int* info;          /* batch */
   atomic_long next;
 } job_t;
@@ -78,6 +85,12 @@ static void* worker(void* arg) {
     if (k0 >= J->batch) break;
     long k1 = k0 + 16 < J->batch ? k0 + 16 : J->batch;
     for (long k = k0; k < k1; ++k) {
+      if (J->mode == 3) { /* real: A holds batch * n * n doubles */
+        memcpy(a, J->A + (size_t)k * n * n, sizeof(double) * (size_t)n * n);
+        J->info[k] = g_dgeev(LAPACK_COL_MAJOR_, 'N', 'N', n, a, n, J->w + (size_t)k * n, J->wi + (size_t)k * n, NULL, 1,
+                             NULL, 1);
+        continue;
+      }
       memcpy(a, J->A + (size_t)k * nn2, sizeof(double) * nn2);
       if (J->mode == 0) {
         J->info[k] = g_zgeev(LAPACK_COL_MAJOR_, 'N', 'N', n, a, n, J->w + (size_t)k * n * 2, NULL, 1, NULL, 1);
@@ -115,6 +128,16 @@ static int run(job_t* J, int nthreads, double* seconds) {
 int cpu_zgeev_batched(int n, int batch, const double* A, double* w, int* info, int nthreads, double* seconds) {
   job_t J;
   J.n = n; J.batch = batch; J.mode = 0; J.A = A; J.w = w; J.rconde = NULL; J.vl = NULL; J.vr = NULL; J.info = info;
+  J.wi = NULL;
+  return run(&J, nthreads, seconds);
+}
+
+/* Real eigenvalues with dgeev('N','N'): A is batch * n * n doubles, column-major. */
+int cpu_dgeev_batched(int n, int batch, const double* A, double* wr, double* wi, int* info, int nthreads,
+                      double* seconds) {
+  job_t J;
+  J.n = n; J.batch = batch; J.mode = 3; J.A = A; J.w = wr; J.wi = wi; J.rconde = NULL; J.vl = NULL; J.vr = NULL;
+  J.info = info;
   return run(&J, nthreads, seconds);
 }
 
@@ -123,6 +146,7 @@ int cpu_zgeev_vectors_batched(int n, int batch, const double* A, double* w, doub
                               int nthreads, double* seconds) {
   job_t J;
   J.n = n; J.batch = batch; J.mode = 2; J.A = A; J.w = w; J.rconde = NULL; J.vl = vl; J.vr = vr; J.info = info;
+  J.wi = NULL;
   return run(&J, nthreads, seconds);
 }
 
@@ -131,5 +155,6 @@ int cpu_zgeevx_batched(int n, int batch, const double* A, double* w, double* rco
                        double* seconds) {
   job_t J;
   J.n = n; J.batch = batch; J.mode = 1; J.A = A; J.w = w; J.rconde = rconde; J.vl = NULL; J.vr = NULL; J.info = info;
+  J.wi = NULL;
   return run(&J, nthreads, seconds);
 }

@@ -79,6 +79,8 @@ def _load():
                                            ctypes.POINTER(ctypes.c_double)]
         lib.cpu_zgeev_vectors_batched.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 5 + [
             ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
+        lib.cpu_dgeev_batched.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 4 + [
+            ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
         lib.ref_zgeev_batched.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.c_void_p]
         st = lib.cpu_zgeev_open(find_lapack().encode())
@@ -115,6 +117,40 @@ def zgeev(A: np.ndarray, threads: int | None = None):
     lib.cpu_zgeev_batched(n, b, A.ctypes.data, w.ctypes.data, info.ctypes.data, threads or default_threads(),
                           ctypes.byref(sec))
     return w, info, sec.value
+
+
+def dgeev(A: np.ndarray, threads: int | None = None):
+    """LAPACK dgeev('N','N') per real matrix (``A[k]`` read as a column-major
+    buffer). Returns ``(wr[batch, n], wi[batch, n], info[batch], seconds)``."""
+    lib = _load()
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    if A.ndim == 2:
+        A = A[None]
+    b, n, _ = A.shape
+    wr = np.empty((b, n), np.float64)
+    wi = np.empty((b, n), np.float64)
+    info = np.empty(b, np.int32)
+    sec = ctypes.c_double()
+    lib.cpu_dgeev_batched(n, b, A.ctypes.data, wr.ctypes.data, wi.ctypes.data, info.ctypes.data,
+                          threads or default_threads(), ctypes.byref(sec))
+    return wr, wi, info, sec.value
+
+
+def check_conjugate_pairs(wr: np.ndarray, wi: np.ndarray) -> bool:
+    """LAPACK's real-eigenvalue output convention: wi[k] > 0 starts a pair
+    with (wr[k+1], wi[k+1]) == (wr[k], -wi[k]) exactly; any other entry has
+    wi == 0."""
+    n = wr.shape[-1]
+    for r, im in zip(wr.reshape(-1, n), wi.reshape(-1, n)):
+        k = 0
+        while k < n:
+            if im[k] == 0.0:
+                k += 1
+            elif im[k] > 0.0 and k + 1 < n and r[k + 1] == r[k] and im[k + 1] == -im[k]:
+                k += 2
+            else:
+                return False
+    return True
 
 
 def zgeev_vectors(A: np.ndarray, threads: int | None = None):
@@ -220,3 +256,37 @@ def parity_report(A: np.ndarray, w_test: np.ndarray, flag_test: np.ndarray, thre
         rep["p99_rel_err_well"] = float(np.nanpercentile(rel[well], 99)) if well.any() else float("nan")
     rep["rel_err"] = rel
     return rep
+
+
+def real_parity_report(A: np.ndarray, wr: np.ndarray, wi: np.ndarray, flag_test: np.ndarray,
+                       threads: int | None = None) -> dict:
+    """Compares real-path eigenvalues/flags against LAPACK dgeev on the same
+    real inputs (``A[k]`` column-major buffers), with the eigenvalue condition
+    numbers of zgeevx on the same matrices selecting the well-conditioned ones."""
+    A = np.ascontiguousarray(A, dtype=np.float64)
+    if A.ndim == 2:
+        A = A[None]
+    wr_ref, wi_ref, info, _ = dgeev(A, threads)
+    w_ref = wr_ref + 1j * wi_ref
+    w_test = np.asarray(wr) + 1j * np.asarray(wi)
+    fro = np.sqrt(np.sum(A ** 2, axis=(1, 2)))
+    fro = np.where(fro == 0, 1.0, fro)
+    flag_test = np.asarray(flag_test)
+    ok = (info == 0) & (flag_test == 0)
+    rel = np.full(A.shape[0], np.nan)
+    if ok.any():
+        err = matched_abs_errors(w_test[ok], w_ref[ok])
+        rel[ok] = np.max(err, axis=1) / fro[ok]
+    _, rc, _ = zgeevx_rconde(A.astype(np.complex128), threads)
+    cond = 1.0 / np.maximum(rc, 1e-300)
+    well = ok & (np.max(cond, axis=1) <= COND_MAX)
+    return {
+        "batch": int(A.shape[0]),
+        "flag_mismatch": int(np.sum((info != 0) != (flag_test != 0))),
+        "lapack_fail": int(np.sum(info != 0)),
+        "pairs_ok": bool(check_conjugate_pairs(np.asarray(wr)[ok], np.asarray(wi)[ok])) if ok.any() else True,
+        "max_rel_err": float(np.nanmax(rel)) if ok.any() else float("nan"),
+        "well_conditioned": int(well.sum()),
+        "max_rel_err_well": float(np.nanmax(rel[well])) if well.any() else float("nan"),
+        "rel_err": rel,
+    }

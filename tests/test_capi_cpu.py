@@ -81,6 +81,52 @@ def test_argument_validation_codes(lib):
     assert f(fake, 0, 0, None, None, None, None, 0) == -2
 
 
+def test_layout_entry_points_validation(lib):
+    fake = ctypes.c_void_p(0x1000)  # never dereferenced: every call below fails validation first
+    p = 0x2000
+    f = api.tokura_zgeev_strided_batched_gpu
+    assert f(None, 8, 4, p, 8, 64, p, 8, p, p) == -1
+    assert f(fake, 65, 4, p, 8, 64, p, 8, p, p) == -2
+    assert f(fake, 8, 4, None, 8, 64, p, 8, p, p) == -3
+    assert f(fake, 8, 4, p, 8, 64, None, 8, p, p) == -4
+    assert f(fake, 8, 4, p, 8, 64, p, 8, None, p) == -5
+    assert f(fake, 8, 0, p, 8, 64, p, 8, p, p) == -6
+    assert f(fake, 8, 4, p, 8, 64, p, 8, p, None) == -7
+    assert f(fake, 8, 4, p, 7, 64, p, 8, p, p) == -8
+    assert f(fake, 8, 4, p, 8, -1, p, 8, p, p) == -9
+    assert f(fake, 8, 4, p, 8, 64, p, 7, p, p) == -9
+    g = api.tokura_zgeev_pointer_batched_gpu
+    assert g(None, 8, 4, p, 8, p, p, p) == -1
+    assert g(fake, 0, 4, p, 8, p, p, p) == -2
+    assert g(fake, 8, 4, None, 8, p, p, p) == -3
+    assert g(fake, 8, 4, p, 8, p, p, None) == -7
+    assert g(fake, 8, 4, p, 3, p, p, p) == -8
+    c = api.tokura_cgeev_batched_gpu
+    assert c(None, 8, 4, p, p, p, p) == -1
+    assert c(fake, 65, 4, p, p, p, p) == -2
+    assert c(fake, 8, 4, p, None, p, p) == -4
+    assert c(fake, 8, -1, p, p, p, p) == -6
+
+
+def test_real_entry_points_validation(lib):
+    fake = ctypes.c_void_p(0x1000)  # never dereferenced: every call below fails validation first
+    p = 0x2000
+    for f in (api.tokura_dgeev_batched_gpu, api.tokura_sgeev_batched_gpu):
+        assert f(None, 8, 4, p, p, p, p, p) == -1
+        assert f(fake, 0, 4, p, p, p, p, p) == -2
+        assert f(fake, 65, 4, p, p, p, p, p) == -2
+        assert f(fake, 8, 4, None, p, p, p, p) == -3
+        assert f(fake, 8, 4, p, None, p, p, p) == -4
+        assert f(fake, 8, 4, p, p, None, p, p) == -4
+        assert f(fake, 8, 4, p, p, p, None, p) == -5
+        assert f(fake, 8, 0, p, p, p, p, p) == -6
+        assert f(fake, 8, 4, p, p, p, p, None) == -7
+    ws = api.tokura_get_dgeev_workspacesize
+    assert ws(64, 65536) == 8 * 64 * 64 * 65536
+    assert ws(0, 5) == 2 ** 64 - 1 and ws(8, 0) == 2 ** 64 - 2
+    assert lib.tokuraSetRealConfig(None, 8, 1, 128) == -1
+
+
 def test_create_destroy_null(lib):
     assert lib.tokuraCreate(None) == -1
     assert lib.tokuraDestroy(None) == 0

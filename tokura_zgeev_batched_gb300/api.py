@@ -74,6 +74,24 @@ _SIGNATURES = {
     ),
     "tokura_get_zgeev_ragged_backward_workspacesize": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_longlong]),
     "tokuraLoadTuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
+    "tokura_zgeev_strided_batched_gpu": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong,
+         ctypes.c_void_p, ctypes.c_longlong, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
+    ),
+    "tokura_zgeev_pointer_batched_gpu": (
+        ctypes.c_int,
+        [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p,
+         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p],
+    ),
+    "tokura_get_dgeev_workspacesize": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int]),
+    "tokura_dgeev_batched_gpu": (
+        ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 6),
+    "tokura_sgeev_batched_gpu": (
+        ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 6),
+    "tokuraSetRealConfig": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "tokura_cgeev_batched_gpu": (
+        ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 5),
 }
 
 
@@ -143,6 +161,9 @@ class Handle:
     def set_balancing(self, mode: int) -> int:
         """0 none, 1 permute, 2 scale, 3 both (LAPACK zgeev's default)."""
         return int(lib().tokuraSetBalancing(self.ptr, int(mode)))
+
+    def set_real_config(self, n: int, lanes: int, threads: int) -> int:
+        return int(lib().tokuraSetRealConfig(self.ptr, int(n), int(lanes), int(threads)))
 
     def set_ragged_lanes(self, lanes: int) -> int:
         return int(lib().tokuraSetRaggedLanes(self.ptr, int(lanes)))
@@ -253,6 +274,183 @@ def zgeev_batched(A, handle: Handle | None = None, work=None, stream=None):
     if status != 0:
         raise RuntimeError(f"tokura_zgeev_batched_gpu returned {status}")
     return eig.reshape(*batch_shape, n), flag.reshape(batch_shape)
+
+
+def tokura_zgeev_strided_batched_gpu(handle, n: int, batch_count: int, A: int, lda: int, strideA: int,
+                                     eigenvalues: int, strideW: int, work: int, flag: int, stream: int = 0) -> int:
+    return int(lib().tokura_zgeev_strided_batched_gpu(_ptr(handle), int(n), int(batch_count), A, int(lda),
+                                                      int(strideA), eigenvalues, int(strideW), work, flag, stream))
+
+
+def tokura_zgeev_pointer_batched_gpu(handle, n: int, batch_count: int, Aarray: int, lda: int, eigenvalues: int,
+                                     work: int, flag: int, stream: int = 0) -> int:
+    return int(lib().tokura_zgeev_pointer_batched_gpu(_ptr(handle), int(n), int(batch_count), Aarray, int(lda),
+                                                      eigenvalues, work, flag, stream))
+
+
+def tokura_cgeev_batched_gpu(handle, n: int, batch_count: int, A: int, eigenvalues: int, work: int, flag: int,
+                             stream: int = 0) -> int:
+    return int(lib().tokura_cgeev_batched_gpu(_ptr(handle), int(n), int(batch_count), A, eigenvalues, work, flag,
+                                              stream))
+
+
+def _column_major_view(M):
+    """(leading dimension, transposed?) for a CUDA matrix view whose rows or
+    columns are unit-stride, or None. eig(M^T) = eig(M), so a row-major view
+    is read as the column-major view of M^T."""
+    r, c = M.stride(-2), M.stride(-1)
+    n = M.shape[-1]
+    if n == 1:
+        return 1, False
+    if r == 1 and c >= n:
+        return c, False
+    if c == 1 and r >= n:
+        return r, True
+    return None
+
+
+def zgeev_strided(A, handle: Handle | None = None, work=None, stream=None):
+    """Eigenvalues of a 3-D complex128 CUDA tensor ``A[b, n, n]`` read in place
+    through its strides (e.g. ``big[:, :n, :n]`` sub-blocks or an expanded
+    single matrix), via tokura_zgeev_strided_batched_gpu. Falls back to a
+    contiguous copy only when neither matrix dimension is unit-stride.
+    Returns ``(eigenvalues[b, n], flag[b])``.
+    """
+    import torch
+
+    if not A.is_cuda or A.dtype != torch.complex128 or A.dim() != 3 or A.shape[-1] != A.shape[-2]:
+        raise TypeError("A must be a 3-D complex128 CUDA tensor of square matrices")
+    batch, n = A.shape[0], A.shape[-1]
+    view = _column_major_view(A)
+    if view is None or A.stride(0) < 0:
+        A = A.contiguous()
+        view = _column_major_view(A)
+    lda = view[0]
+    eig = torch.empty(batch, n, dtype=torch.complex128, device=A.device)
+    flag = torch.empty(batch, dtype=torch.int8, device=A.device)
+    if batch == 0:
+        return eig, flag
+    need = tokura_get_zgeeveigenvaluesgetworspacesize(n, batch)
+    if work is None or work.numel() * work.element_size() < need:
+        work = torch.empty(need, dtype=torch.uint8, device=A.device)
+    s = stream if stream is not None else torch.cuda.current_stream(A.device)
+    h = handle if handle is not None else default_handle()
+    st = tokura_zgeev_strided_batched_gpu(h, n, batch, A.data_ptr(), lda, A.stride(0) if batch > 1 else 0,
+                                          eig.data_ptr(), n, work.data_ptr(), flag.data_ptr(), s.cuda_stream)
+    if st != 0:
+        raise RuntimeError(f"tokura_zgeev_strided_batched_gpu returned {st}")
+    return eig, flag
+
+
+def zgeev_pointers(mats, handle: Handle | None = None, work=None, stream=None):
+    """Eigenvalues of a list of complex128 CUDA matrices (each ``[n, n]``, any
+    addresses, one common leading dimension) via the pointer-array entry point.
+    ``None`` entries are passed as NULL pointers (flag 3, NaN eigenvalues).
+    Returns ``(eigenvalues[len, n], flag[len])``.
+    """
+    import torch
+
+    present = [m for m in mats if m is not None]
+    if not present:
+        raise ValueError("need at least one matrix")
+    dev = present[0].device
+    n = present[0].shape[-1]
+    views = {_column_major_view(m) for m in present}
+    if len(views) != 1 or None in views or any(m.shape != (n, n) or m.dtype != torch.complex128 for m in present):
+        raise ValueError("matrices must be complex128 [n, n] views sharing one leading dimension")
+    lda = views.pop()[0]
+    batch = len(mats)
+    ptrs = torch.tensor([m.data_ptr() if m is not None else 0 for m in mats], dtype=torch.int64).to(dev)
+    eig = torch.empty(batch, n, dtype=torch.complex128, device=dev)
+    flag = torch.empty(batch, dtype=torch.int8, device=dev)
+    need = tokura_get_zgeeveigenvaluesgetworspacesize(n, batch)
+    if work is None or work.numel() * work.element_size() < need:
+        work = torch.empty(need, dtype=torch.uint8, device=dev)
+    s = stream if stream is not None else torch.cuda.current_stream(dev)
+    h = handle if handle is not None else default_handle()
+    st = tokura_zgeev_pointer_batched_gpu(h, n, batch, ptrs.data_ptr(), lda, eig.data_ptr(), work.data_ptr(),
+                                          flag.data_ptr(), s.cuda_stream)
+    if st != 0:
+        raise RuntimeError(f"tokura_zgeev_pointer_batched_gpu returned {st}")
+    return eig, flag
+
+
+def cgeev_batched(A, handle: Handle | None = None, work=None, stream=None):
+    """Eigenvalues of complex64 CUDA matrices ``A[..., n, n]``, computed in FP64
+    and returned as complex64 (tokura_cgeev_batched_gpu). Returns
+    ``(eigenvalues[..., n], flag[...])``."""
+    import torch
+
+    if not A.is_cuda or A.dtype != torch.complex64:
+        raise TypeError("A must be a complex64 CUDA tensor")
+    n = A.shape[-1]
+    if A.shape[-2] != n:
+        raise ValueError("matrices must be square")
+    batch_shape = A.shape[:-2]
+    Ab = A.reshape(-1, n, n).contiguous()
+    batch = Ab.shape[0]
+    eig = torch.empty(batch, n, dtype=torch.complex64, device=A.device)
+    flag = torch.empty(batch, dtype=torch.int8, device=A.device)
+    if batch == 0:
+        return eig.reshape(*batch_shape, n), flag.reshape(batch_shape)
+    need = tokura_get_zgeeveigenvaluesgetworspacesize(n, batch)
+    if work is None or work.numel() * work.element_size() < need:
+        work = torch.empty(need, dtype=torch.uint8, device=A.device)
+    s = stream if stream is not None else torch.cuda.current_stream(A.device)
+    h = handle if handle is not None else default_handle()
+    st = tokura_cgeev_batched_gpu(h, n, batch, Ab.data_ptr(), eig.data_ptr(), work.data_ptr(), flag.data_ptr(),
+                                  s.cuda_stream)
+    if st != 0:
+        raise RuntimeError(f"tokura_cgeev_batched_gpu returned {st}")
+    return eig.reshape(*batch_shape, n), flag.reshape(batch_shape)
+
+
+def tokura_get_dgeev_workspacesize(n: int, batch_count: int) -> int:
+    return int(lib().tokura_get_dgeev_workspacesize(int(n), int(batch_count)))
+
+
+def tokura_dgeev_batched_gpu(handle, n: int, batch_count: int, A: int, wr: int, wi: int, work: int, flag: int,
+                             stream: int = 0) -> int:
+    return int(lib().tokura_dgeev_batched_gpu(_ptr(handle), int(n), int(batch_count), A, wr, wi, work, flag, stream))
+
+
+def tokura_sgeev_batched_gpu(handle, n: int, batch_count: int, A: int, wr: int, wi: int, work: int, flag: int,
+                             stream: int = 0) -> int:
+    return int(lib().tokura_sgeev_batched_gpu(_ptr(handle), int(n), int(batch_count), A, wr, wi, work, flag, stream))
+
+
+def dgeev_batched(A, handle: Handle | None = None, work=None, stream=None):
+    """Eigenvalues of real CUDA matrices ``A[..., n, n]`` (float64 -> dgeev
+    path, float32 -> sgeev path, FP64 inside). Returns ``(wr, wi, flag)`` in
+    LAPACK's convention (conjugate pairs adjacent, positive imaginary part
+    first). Matrices are taken as stored by torch (row-major); eig(M^T) =
+    eig(M), so the spectrum is that of A.
+    """
+    import torch
+
+    if not A.is_cuda or A.dtype not in (torch.float64, torch.float32):
+        raise TypeError("A must be a float64 or float32 CUDA tensor")
+    n = A.shape[-1]
+    if A.shape[-2] != n:
+        raise ValueError("matrices must be square")
+    batch_shape = A.shape[:-2]
+    Ab = A.reshape(-1, n, n).contiguous()
+    batch = Ab.shape[0]
+    wr = torch.empty(batch, n, dtype=A.dtype, device=A.device)
+    wi = torch.empty(batch, n, dtype=A.dtype, device=A.device)
+    flag = torch.empty(batch, dtype=torch.int8, device=A.device)
+    if batch > 0:
+        need = tokura_get_dgeev_workspacesize(n, batch)
+        if work is None or work.numel() * work.element_size() < need:
+            work = torch.empty(need, dtype=torch.uint8, device=A.device)
+        s = stream if stream is not None else torch.cuda.current_stream(A.device)
+        h = handle if handle is not None else default_handle()
+        fn = tokura_dgeev_batched_gpu if A.dtype == torch.float64 else tokura_sgeev_batched_gpu
+        st = fn(h, n, batch, Ab.data_ptr(), wr.data_ptr(), wi.data_ptr(), work.data_ptr(), flag.data_ptr(),
+                s.cuda_stream)
+        if st != 0:
+            raise RuntimeError(f"{fn.__name__} returned {st}")
+    return wr.reshape(*batch_shape, n), wi.reshape(*batch_shape, n), flag.reshape(batch_shape)
 
 
 def probe_fp64_peak(device=None) -> float:

@@ -29,6 +29,8 @@ SOURCES = [
     "zgeev_plain.cu",
     "peak_probe.cu",
     "zgeev_noalloc.cu",
+    "zgeev_layouts.cu",
+    "dgeev_batched.cu",
     "zgeev_ragged.cu",
     "tokura_tuner.cu",
     "zgeev_backward.cu",

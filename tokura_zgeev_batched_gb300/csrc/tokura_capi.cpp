@@ -88,6 +88,18 @@ extern "C" int tokuraSetPlainConfig(tokurablas_t* handle, int n, int lanes_per_m
   return 0;
 }
 
+extern "C" int tokuraSetRealConfig(tokurablas_t* handle, int n, int lanes_per_matrix, int threads_per_block) {
+  if (handle == nullptr) return -1;
+  if (!(n > 0 && n <= TOKURA_ZGEEV_BATCHED_MAX_MATRIX_SIZE)) return -2;
+  if (!(lanes_per_matrix == 0 || lanes_per_matrix == 1 || lanes_per_matrix == 2 || lanes_per_matrix == 4 ||
+        lanes_per_matrix == 8))
+    return -3;
+  if (!(threads_per_block == 0 || (threads_per_block >= 32 && threads_per_block <= 256 && threads_per_block % 32 == 0)))
+    return -4;
+  handle->real[n] = PlainConfig{lanes_per_matrix, threads_per_block};
+  return 0;
+}
+
 extern "C" int tokuraGetPlainConfig(const tokurablas_t* handle, int n, int batch_count, int* lanes_per_matrix,
                                     int* threads_per_block) {
   if (handle == nullptr || lanes_per_matrix == nullptr || threads_per_block == nullptr) return -1;

@@ -28,6 +28,7 @@ struct tokurablas_t {
   int itmax_override = 0;  // >0 replaces the per-eigenvalue sweep cap 30*max(10,n)
   // Tuned plain-kernel shape per n (index 1..64); lanes == 0 means "heuristic".
   tzg::PlainConfig plain[65] = {};
+  tzg::PlainConfig real[65] = {};  // the same for the real (dgeev/sgeev) kernel
   int ragged_lanes = 0;  // lanes per matrix of the ragged solvers; 0 = chosen per launch
   int balance_mode = 0;  // balancing before the eigenvalue solves: 0 none (the reference's behaviour) .. 3 both
   tzg::HostPipeline pipe;  // host-buffer entry point state (guarded by pipe_mutex)
@@ -38,6 +39,7 @@ namespace tzg {
 
 inline void init_default_tuning(tokurablas_t* h) {
   for (int n = 0; n <= 64; ++n) h->plain[n] = PlainConfig{0, 128};
+  for (int n = 0; n <= 64; ++n) h->real[n] = PlainConfig{0, 128};
 }
 
 // Lanes per matrix: enough lane groups to give every SM sub-partition at
@@ -53,6 +55,19 @@ inline PlainConfig plain_config_for(const tokurablas_t* h, int n, int batch) {
       c.lanes = 2;
     else
       c.lanes = 4;
+    if (n <= 2) c.lanes = 1;
+  }
+  if (c.threads == 0) c.threads = 128;
+  return c;
+}
+
+// Launch shape of the real kernel: a tuned entry, else the lane heuristic of
+// the complex kernel (it depends on the batch size, not on the arithmetic).
+inline PlainConfig real_config_for(const tokurablas_t* h, int n, int batch) {
+  PlainConfig c = h->real[n];
+  if (c.lanes == 0) {
+    const long long want_lanes = (long long)h->sm_count * 4 * 2 * 32;
+    c.lanes = (long long)batch >= want_lanes ? 1 : ((long long)batch * 2 >= want_lanes ? 2 : 4);
     if (n <= 2) c.lanes = 1;
   }
   if (c.threads == 0) c.threads = 128;

@@ -15,18 +15,46 @@ namespace tzg {
 // which is the reference's contract, tokura_zhseqr_MWB_kernel.cuh:768-776).
 enum : int { kConverged = 0, kNotConverged = 1, kNonFinite = 2, kInvalidInput = 3 };
 
-// Stage matrix `slot` of a tile from column-major `src` (n*n elements) into
-// the tile-interleaved view, scaling by an exact power of two when the
-// largest |Re|,|Im| lies outside [2^-60, 2^60] (zgeev's pre-scaling,
-// done exactly). Returns the applied exponent shift (eigenvalues are
-// multiplied by 2^shift on output), or sets `nonfinite`.
-template <int L>
-__device__ __forceinline__ int stage_and_scale(const double2* __restrict__ src, const MatView& M,
-                                               const Group<L>& G, bool& nonfinite, bool& zero) {
-  const int nn = M.n * M.n;
+// Sources of the matrix entries, addressed by the column-major linear index
+// e = r + c*n of an n x n matrix (all loads are read-only, no alignment
+// demands beyond the element type's).
+struct SrcContig {  // n x n column-major, contiguous (the reference's layout)
+  const double2* p;
+  __device__ __forceinline__ double2 load(int e, int) const { return p[e]; }
+};
+struct SrcStrided {  // column-major with leading dimension ld >= n
+  const double2* p;
+  long long ld;
+  __device__ __forceinline__ double2 load(int e, int n) const {
+    const int c = e / n;
+    return p[(e - c * n) + c * ld];
+  }
+};
+struct SrcComplex64 {  // contiguous single-precision complex, widened on load
+  const float2* p;
+  __device__ __forceinline__ double2 load(int e, int) const {
+    const float2 z = p[e];
+    return make_double2((double)z.x, (double)z.y);
+  }
+};
+
+// Eigenvalue stores: full precision, or rounded to single precision.
+__device__ __forceinline__ void put_ev(double2* p, double2 v) { *p = v; }
+__device__ __forceinline__ void put_ev(float2* p, double2 v) { *p = make_float2((float)v.x, (float)v.y); }
+
+// Stage matrix `slot` of a tile from `src` into the tile-interleaved view,
+// scaling by an exact power of two when the largest |Re|,|Im| lies outside
+// [2^-60, 2^60] (zgeev's pre-scaling, done exactly). Returns the applied
+// exponent shift (eigenvalues are multiplied by 2^shift on output), or sets
+// `nonfinite`.
+template <int L, class Src>
+__device__ __forceinline__ int stage_and_scale(const Src& src, const MatView& M, const Group<L>& G, bool& nonfinite,
+                                               bool& zero) {
+  const int n = M.n;
+  const int nn = n * n;
   int emax = 0;
   for (int e = G.rank; e < nn; e += L) {
-    const double2 z = src[e];
+    const double2 z = src.load(e, n);
     emax = max(emax, max(dexp_field(z.x), dexp_field(z.y)));
   }
   emax = G.imax(emax);
@@ -38,16 +66,23 @@ __device__ __forceinline__ int stage_and_scale(const double2* __restrict__ src, 
     if (top > 60 || top < -60) shift = top;
   }
   if (shift == 0) {
-    for (int e = G.rank; e < nn; e += L) M.p[e * M.rs] = src[e];
+    for (int e = G.rank; e < nn; e += L) M.p[e * M.rs] = src.load(e, n);
   } else {
     const double sc = pow2(-shift);
     for (int e = G.rank; e < nn; e += L) {
-      const double2 z = src[e];
+      const double2 z = src.load(e, n);
       M.p[e * M.rs] = make_double2(z.x * sc, z.y * sc);
     }
   }
   G.sync();
   return shift;
+}
+
+// Column-major contiguous source (the reference's layout).
+template <int L>
+__device__ __forceinline__ int stage_and_scale(const double2* __restrict__ src, const MatView& M,
+                                               const Group<L>& G, bool& nonfinite, bool& zero) {
+  return stage_and_scale<L>(SrcContig{src}, M, G, nonfinite, zero);
 }
 
 // Applies P = I - tau v v^H (v[0] = 1, v[i] at x[i*xs]) to NV vectors of
@@ -107,30 +142,40 @@ __device__ __forceinline__ void reflect_vectors(double2* const (&p)[NV], const d
 // Balancing modes (LAPACK zgebal's JOB): none, permute only, scale only, both.
 enum : int { kBalanceNone = 0, kBalancePermute = 1, kBalanceScale = 2, kBalanceBoth = 3 };
 
+// Element helpers shared by the complex (double2) and real (double) views.
+__device__ __forceinline__ bool is_zero(double2 z) {
+  const unsigned long long bits =
+      (unsigned long long)__double_as_longlong(z.x) | (unsigned long long)__double_as_longlong(z.y);
+  return (bits << 1) == 0;  // ignores the sign bits: -0.0 counts as zero
+}
+__device__ __forceinline__ bool is_zero(double x) { return ((unsigned long long)__double_as_longlong(x) << 1) == 0; }
+__device__ __forceinline__ double acc_abs2(double acc, double2 a) { return fma(a.x, a.x, fma(a.y, a.y, acc)); }
+__device__ __forceinline__ double acc_abs2(double acc, double a) { return fma(a, a, acc); }
+__device__ __forceinline__ double2 scaled(double2 a, double f) { return make_double2(a.x * f, a.y * f); }
+__device__ __forceinline__ double scaled(double a, double f) { return a * f; }
+
 // True if every entry of row (kRow) / column j inside [lo, hi], other than
 // the diagonal, is exactly zero (bit test, no FP64 work).
-template <bool kRow>
-__device__ __forceinline__ bool offdiag_zero(const MatView& M, int j, int lo, int hi) {
+template <bool kRow, class View>
+__device__ __forceinline__ bool offdiag_zero(const View& M, int j, int lo, int hi) {
   for (int k = lo; k <= hi; ++k) {
     if (k == j) continue;
-    const double2 z = kRow ? *M.at(j, k) : *M.at(k, j);
-    const unsigned long long bits =
-        (unsigned long long)__double_as_longlong(z.x) | (unsigned long long)__double_as_longlong(z.y);
-    if ((bits << 1) != 0) return false;  // ignores the sign bit: -0.0 counts as zero
+    if (!is_zero(kRow ? *M.at(j, k) : *M.at(k, j))) return false;
   }
   return true;
 }
 
 // Swaps rows and columns a and b (a similarity by a permutation).
-__device__ __forceinline__ void swap_rc(const MatView& M, int a, int b) {
+template <class View>
+__device__ __forceinline__ void swap_rc(const View& M, int a, int b) {
   if (a == b) return;
   for (int k = 0; k < M.n; ++k) {
-    const double2 t = *M.at(k, a);
+    const auto t = *M.at(k, a);
     *M.at(k, a) = *M.at(k, b);
     *M.at(k, b) = t;
   }
   for (int k = 0; k < M.n; ++k) {
-    const double2 t = *M.at(a, k);
+    const auto t = *M.at(a, k);
     *M.at(a, k) = *M.at(b, k);
     *M.at(b, k) = t;
   }
@@ -145,8 +190,8 @@ __device__ __forceinline__ void swap_rc(const MatView& M, int a, int b) {
 // least 5 %. Eigenvalues are unchanged; the isolated ones deflate at once in
 // the QR. The permutation search (bit tests only) runs on rank 0; the norms
 // and the row/column scaling of each index are split across the group.
-template <int L>
-__device__ void balance(const MatView& M, const Group<L>& G, int mode) {
+template <int L, class View>
+__device__ void balance(const View& M, const Group<L>& G, int mode) {
   const int n = M.n;
   int lo = 0, hi = n - 1;
   if (mode & kBalancePermute) {
@@ -187,9 +232,8 @@ __device__ void balance(const MatView& M, const Group<L>& G, int mode) {
     for (int i = lo; i <= hi; ++i) {
       double c = 0.0, r = 0.0;
       for (int k = lo + G.rank; k <= hi; k += L) {
-        const double2 a = *M.at(k, i), b = *M.at(i, k);
-        c = fma(a.x, a.x, fma(a.y, a.y, c));
-        r = fma(b.x, b.x, fma(b.y, b.y, r));
+        c = acc_abs2(c, *M.at(k, i));
+        r = acc_abs2(r, *M.at(i, k));
       }
       c = G.sum(c);
       r = G.sum(r);
@@ -207,10 +251,10 @@ __device__ void balance(const MatView& M, const Group<L>& G, int mode) {
       noconv = true;
       const double f = pow2(e), g = pow2(-e);
       for (int k = G.rank; k < n; k += L) {  // column i times f, row i times 1/f
-        double2* a = M.at(k, i);
-        *a = make_double2(a->x * f, a->y * f);
-        double2* b = M.at(i, k);
-        *b = make_double2(b->x * g, b->y * g);
+        auto* a = M.at(k, i);
+        *a = scaled(*a, f);
+        auto* b = M.at(i, k);
+        *b = scaled(*b, g);
       }
       G.sync();
     }
@@ -328,9 +372,8 @@ __device__ __forceinline__ bool negligible_subdiag(const MatView& M, int k, int 
 // the bottom up. On return eig_out[i] holds the i-th Schur diagonal entry
 // (times 2^shift). Returns kConverged or kNotConverged. The per-eigenvalue
 // sweep cap defaults to LAPACK's 30*max(10, n).
-template <int L>
-__device__ int qr_eigenvalues(const MatView& M, const Group<L>& G, double2* __restrict__ eig_out, int shift,
-                              int itmax) {
+template <int L, class Out = double2>
+__device__ int qr_eigenvalues(const MatView& M, const Group<L>& G, Out* __restrict__ eig_out, int shift, int itmax) {
   const int n = M.n;
   const int rs = M.rs;
   const int cs = n * rs;
@@ -361,7 +404,7 @@ __device__ int qr_eigenvalues(const MatView& M, const Group<L>& G, double2* __re
       if (lo < i) break;
       if (G.rank == 0) {
         const double2 d = *M.at(i, i);
-        eig_out[i] = make_double2(d.x * unscale, d.y * unscale);
+        put_ev(eig_out + i, make_double2(d.x * unscale, d.y * unscale));
       }
       i -= 1;
       lo = 0;
@@ -429,7 +472,7 @@ __device__ int qr_eigenvalues(const MatView& M, const Group<L>& G, double2* __re
     // Unconverged positions 0..i carry their current diagonal entries.
     for (int k = 0; k <= i; ++k) {
       const double2 d = *M.at(k, k);
-      eig_out[k] = make_double2(d.x * unscale, d.y * unscale);
+      put_ev(eig_out + k, make_double2(d.x * unscale, d.y * unscale));
     }
   }
   return status;
@@ -439,19 +482,26 @@ __device__ int qr_eigenvalues(const MatView& M, const Group<L>& G, double2* __re
 // Hessenberg reduction, QR, eigenvalue write-out. Returns the flag value.
 // kBalance selects the instantiation that runs balance() with balance_mode;
 // without it the balancing code is not compiled into the kernel at all.
-template <int L, bool kBalance = false>
-__device__ __forceinline__ int solve_matrix(const double2* __restrict__ src, const MatView& M, const Group<L>& G,
-                                            double2* __restrict__ ev, int itmax, int balance_mode = kBalanceNone) {
+template <int L, bool kBalance = false, class Src = SrcContig, class Out = double2>
+__device__ __forceinline__ int solve_matrix(const Src& src, const MatView& M, const Group<L>& G,
+                                            Out* __restrict__ ev, int itmax, int balance_mode = kBalanceNone) {
   bool nonfinite, zero;
   const int shift = stage_and_scale<L>(src, M, G, nonfinite, zero);
   if (nonfinite || zero) {
     const double v = nonfinite ? __longlong_as_double(0x7ff8000000000000LL) : 0.0;
-    for (int i = G.rank; i < M.n; i += L) ev[i] = make_double2(v, v);
+    for (int i = G.rank; i < M.n; i += L) put_ev(ev + i, make_double2(v, v));
     return nonfinite ? kNonFinite : kConverged;
   }
   if (kBalance) balance<L>(M, G, balance_mode);
   hessenberg<L>(M, G);
   return qr_eigenvalues<L>(M, G, ev, shift, itmax);
+}
+
+// Contiguous column-major double-complex source (the reference's layout).
+template <int L, bool kBalance = false>
+__device__ __forceinline__ int solve_matrix(const double2* __restrict__ src, const MatView& M, const Group<L>& G,
+                                            double2* __restrict__ ev, int itmax, int balance_mode = kBalanceNone) {
+  return solve_matrix<L, kBalance, SrcContig, double2>(SrcContig{src}, M, G, ev, itmax, balance_mode);
 }
 
 }  // namespace tzg
