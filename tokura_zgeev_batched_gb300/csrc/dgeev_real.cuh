@@ -371,10 +371,15 @@ __device__ int real_qr_eigenvalues(const RMatView& M, const Group<L>& G, Out* __
     {
       int hit = l;
       for (int c = i - 2 - G.rank; c > l; c -= L) {
-        double v1, v2, v3;
-        double_shift_vector(M, c, rt1r, rt1i, rt2r, rt2i, v1, v2, v3);
-        const double h00 = fabs(*M.at(c, c - 1)) * (fabs(v2) + fabs(v3));
-        const double h01 = fabs(v1) * (fabs(*M.at(c - 1, c - 1)) + fabs(*M.at(c, c)) + fabs(*M.at(c + 1, c + 1)));
+        // The test is invariant under scaling of v, so the unnormalized
+        // s*v (no divisions) serves; entries of the pre-scaled matrix keep
+        // the products far from overflow.
+        const double hcc = *M.at(c, c), h21 = *M.at(c + 1, c), h22 = *M.at(c + 1, c + 1);
+        const double u1 = fma(h21, *M.at(c, c + 1), fma(hcc - rt1r, hcc - rt2r, -rt1i * rt2i));
+        const double u2 = h21 * (hcc + h22 - rt1r - rt2r);
+        const double u3 = h21 * *M.at(c + 2, c + 1);
+        const double h00 = fabs(*M.at(c, c - 1)) * (fabs(u2) + fabs(u3));
+        const double h01 = fabs(u1) * (fabs(*M.at(c - 1, c - 1)) + fabs(hcc) + fabs(h22));
         if (h00 <= kUlp * h01) {
           hit = c;
           break;
@@ -394,15 +399,27 @@ __device__ int real_qr_eigenvalues(const RMatView& M, const Group<L>& G, Out* __
       } else if (nr == 2) {
         v3 = 0.0;
       }
+      // Reflector (dlarfg's): beta = -sign(v1) ||v||, t1 = (beta - v1)/beta
+      // = 1 + |v1|/||v||, v(2:3) /= (v1 - beta). One rsqrt and one
+      // reciprocal; tiny or huge norms take the hypot route.
       double t1 = 0.0;
-      const double xnorm = nr == 3 ? hypot(v2, v3) : fabs(v2);
-      if (xnorm != 0.0) {
-        const double beta = -copysign(hypot(v1, xnorm), v1);
-        t1 = (beta - v1) / beta;
-        const double scal = 1.0 / (v1 - beta);
+      const double ss = fma(v2, v2, v3 * v3);
+      if (ss != 0.0) {
+        const double nn = fma(v1, v1, ss);
+        double xn, rxn;
+        if (nn > 1e-280 && nn < 1e280) {
+          rxn = rsqrt(nn);
+          xn = nn * rxn;
+        } else {
+          xn = hypot(v1, hypot(v2, v3));
+          rxn = 1.0 / xn;
+        }
+        const double a1 = fabs(v1);
+        t1 = fma(a1, rxn, 1.0);
+        const double scal = copysign(1.0 / (a1 + xn), v1);
         v2 *= scal;
         v3 *= scal;
-        v1 = beta;
+        v1 = -copysign(xn, v1);
       }
       G.sync();  // every lane has read column k-1 before it changes
       if (G.rank == 0) {

@@ -9,14 +9,14 @@ namespace tzg {
 
 // Device buffers and streams of the host-buffer entry point, cached per handle.
 struct HostPipeline {
-  static constexpr int kStreams = 4;
+  static constexpr int kStreams = 16;  // at most one stream per chunk in flight
   void* d_a[kStreams] = {};
   void* d_eig[kStreams] = {};
   void* d_work[kStreams] = {};
   char* d_flag[kStreams] = {};
   cudaStream_t stream[kStreams] = {};
   cudaEvent_t done = nullptr;
-  size_t cap_a = 0, cap_eig = 0, cap_work = 0, cap_flag = 0;
+  size_t cap_a[kStreams] = {}, cap_eig[kStreams] = {}, cap_work[kStreams] = {}, cap_flag[kStreams] = {};
   void release();
 };
 
@@ -38,13 +38,17 @@ struct tokurablas_t {
 namespace tzg {
 
 inline void init_default_tuning(tokurablas_t* h) {
-  for (int n = 0; n <= 64; ++n) h->plain[n] = PlainConfig{0, 128};
-  for (int n = 0; n <= 64; ++n) h->real[n] = PlainConfig{0, 128};
+  for (int n = 0; n <= 64; ++n) h->plain[n] = PlainConfig{0, 0};
+  for (int n = 0; n <= 64; ++n) h->real[n] = PlainConfig{0, 0};
 }
 
 // Lanes per matrix: enough lane groups to give every SM sub-partition at
 // least two warps (FP64 saturates at one warp per sub-partition; the second
 // hides memory latency); otherwise spread each matrix over more lanes.
+// Blocks of 64 threads: when the whole batch is resident at once, the block
+// is the unit the hardware spreads over the SMs, so small blocks even out
+// the per-SM load (at n = 64, 65536 matrices: 2048 warps over 152 SMs run
+// about 11 % faster in 64-thread blocks than in 128-thread blocks).
 inline PlainConfig plain_config_for(const tokurablas_t* h, int n, int batch) {
   PlainConfig c = h->plain[n];
   if (c.lanes == 0) {
@@ -57,7 +61,7 @@ inline PlainConfig plain_config_for(const tokurablas_t* h, int n, int batch) {
       c.lanes = 4;
     if (n <= 2) c.lanes = 1;
   }
-  if (c.threads == 0) c.threads = 128;
+  if (c.threads == 0) c.threads = 64;
   return c;
 }
 
@@ -70,7 +74,7 @@ inline PlainConfig real_config_for(const tokurablas_t* h, int n, int batch) {
     c.lanes = (long long)batch >= want_lanes ? 1 : ((long long)batch * 2 >= want_lanes ? 2 : 4);
     if (n <= 2) c.lanes = 1;
   }
-  if (c.threads == 0) c.threads = 128;
+  if (c.threads == 0) c.threads = 64;
   return c;
 }
 

@@ -31,7 +31,7 @@ void HostPipeline::release() {
   }
   if (done) cudaEventDestroy(done);
   done = nullptr;
-  cap_a = cap_eig = cap_work = cap_flag = 0;
+  for (int s = 0; s < kStreams; ++s) cap_a[s] = cap_eig[s] = cap_work[s] = cap_flag[s] = 0;
 }
 
 static cudaError_t grow(void** p, size_t* cap, size_t need) {
@@ -44,26 +44,24 @@ static cudaError_t grow(void** p, size_t* cap, size_t need) {
   return err;
 }
 
-static cudaError_t ensure(HostPipeline& P, int n, int chunk) {
+static cudaError_t ensure(HostPipeline& P, int n, int chunk, int streams) {
   cudaError_t err;
-  for (int s = 0; s < HostPipeline::kStreams; ++s) {
+  for (int s = 0; s < streams; ++s) {
     if (!P.stream[s] && (err = cudaStreamCreateWithFlags(&P.stream[s], cudaStreamNonBlocking)) != cudaSuccess)
       return err;
   }
   if (!P.done && (err = cudaEventCreateWithFlags(&P.done, cudaEventDisableTiming)) != cudaSuccess) return err;
   const size_t a = sizeof(double2) * (size_t)n * n * chunk;
   const size_t e = sizeof(double2) * (size_t)n * chunk;
-  for (int s = 0; s < HostPipeline::kStreams; ++s) {
-    size_t ca = P.cap_a, ce = P.cap_eig, cw = P.cap_work, cf = P.cap_flag;
-    if ((err = grow(&P.d_a[s], &ca, a)) != cudaSuccess) return err;
-    if ((err = grow(&P.d_eig[s], &ce, e)) != cudaSuccess) return err;
-    if ((err = grow(&P.d_work[s], &cw, a)) != cudaSuccess) return err;
-    if ((err = grow(reinterpret_cast<void**>(&P.d_flag[s]), &cf, (size_t)chunk)) != cudaSuccess) return err;
+  // Buffers of every stream grow to the largest chunk seen; caps are per
+  // stream so a later call with more streams allocates the new ones.
+  for (int s = 0; s < streams; ++s) {
+    if ((err = grow(&P.d_a[s], &P.cap_a[s], a)) != cudaSuccess) return err;
+    if ((err = grow(&P.d_eig[s], &P.cap_eig[s], e)) != cudaSuccess) return err;
+    if ((err = grow(&P.d_work[s], &P.cap_work[s], a)) != cudaSuccess) return err;
+    if ((err = grow(reinterpret_cast<void**>(&P.d_flag[s]), &P.cap_flag[s], (size_t)chunk)) != cudaSuccess)
+      return err;
   }
-  if (a > P.cap_a) P.cap_a = a;
-  if (e > P.cap_eig) P.cap_eig = e;
-  if (a > P.cap_work) P.cap_work = a;
-  if ((size_t)chunk > P.cap_flag) P.cap_flag = chunk;
   return cudaSuccess;
 }
 
@@ -80,21 +78,25 @@ extern "C" TOKURA_API int tokura_zgeev_batched_host(tokurablas_t* handle, int n,
   if (flag == nullptr) return -7;
   if (chunk_matrices < 0) return -8;
   using tzg::HostPipeline;
-  // Default chunk: one round over the streams, but at least 1024 matrices per chunk.
+  // Default: 8 chunks (at least 1024 matrices each). Every chunk in flight
+  // has its own stream and buffers (up to 16), so all chunk kernels can be
+  // resident together while later chunks are still being copied in.
   int chunk = chunk_matrices;
   if (chunk == 0) {
-    chunk = (batch_count + HostPipeline::kStreams - 1) / HostPipeline::kStreams;
+    chunk = (batch_count + 7) / 8;
     if (chunk < 1024) chunk = 1024;
   }
   if (chunk > batch_count) chunk = batch_count;
+  const long long chunks = (batch_count + (long long)chunk - 1) / chunk;
+  const int streams = chunks < HostPipeline::kStreams ? (int)chunks : HostPipeline::kStreams;
   std::lock_guard<std::mutex> lock(handle->pipe_mutex);
   HostPipeline& P = handle->pipe;
-  if (tzg::ensure(P, n, chunk) != cudaSuccess) return 2;
+  if (tzg::ensure(P, n, chunk, streams) != cudaSuccess) return 2;
   const int itmax = handle->itmax_override > 0 ? handle->itmax_override : tzg::default_itmax(n);
   const size_t nn = (size_t)n * n;
   int k = 0;
   for (long long first = 0; first < batch_count; first += chunk, ++k) {
-    const int s = k % HostPipeline::kStreams;
+    const int s = k % streams;
     const int m = (int)((batch_count - first) < chunk ? (batch_count - first) : chunk);
     cudaStream_t st = P.stream[s];
     if (cudaMemcpyAsync(P.d_a[s], A + first * nn, sizeof(double2) * nn * m, cudaMemcpyHostToDevice, st) !=
@@ -110,7 +112,7 @@ extern "C" TOKURA_API int tokura_zgeev_batched_host(tokurablas_t* handle, int n,
         cudaMemcpyAsync(flag + first, P.d_flag[s], (size_t)m, cudaMemcpyDeviceToHost, st) != cudaSuccess)
       return 1;
   }
-  for (int s = 0; s < HostPipeline::kStreams; ++s)
+  for (int s = 0; s < streams; ++s)
     if (cudaStreamSynchronize(P.stream[s]) != cudaSuccess) return 1;
   return 0;
 }

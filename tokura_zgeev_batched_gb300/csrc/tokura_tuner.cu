@@ -98,15 +98,15 @@ extern "C" TOKURA_API int tokuraAutotune(tokurablas_t* handle, int n_min, int n_
   double2* work = static_cast<double2*>(b.p[2]);
   char* flag = static_cast<char*>(b.p[3]);
   static const int kLanes[4] = {1, 2, 4, 8};
-  static const int kThreads[3] = {64, 128, 256};
+  static const int kThreads[4] = {32, 64, 128, 256};
   for (int n = n_min; n <= n_max; ++n) {
     const long long count = (long long)n * n * batch_count;
     fill_cgauss_kernel<<<handle->sm_count * 4, 256, 0, stream>>>(A, count, 0x5eed0000ULL + n);
     float best = 1e30f;
-    PlainConfig best_cfg{1, 128};
+    PlainConfig best_cfg{1, 64};
     for (int li = 0; li < 4; ++li) {
       if (n <= 2 && kLanes[li] > 1) continue;
-      for (int ti = 0; ti < 3; ++ti) {
+      for (int ti = 0; ti < 4; ++ti) {
         const PlainConfig cfg{kLanes[li], kThreads[ti]};
         cudaError_t err;
         const float ms = time_launches(stream, 2, [&]() {

@@ -110,7 +110,7 @@ cudaError_t launch_vectors(int lanes, int n, int batch, const double2* A, double
                            double2* work, char* flag, int itmax, cudaStream_t stream) {
   const int tw = 32 / lanes;
   const long long warps = ((long long)batch + tw - 1) / tw;
-  const int threads = 128;
+  const int threads = 64;  // small blocks spread a resident batch evenly over the SMs
   const long long blocks = (warps * 32 + threads - 1) / threads;
   if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
   switch (lanes) {
