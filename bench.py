@@ -264,6 +264,51 @@ def measure_config1(h, dev, stream, peak, call) -> dict:
             "parity": spot_check(A, eig, flag, 256)}
 
 
+def measure_real(h, dev, stream, peak, n: int = 64, batch: int = 65536, cpu_seconds: float = 2.0) -> dict:
+    """Real-input path (tokura_dgeev_batched_gpu): real Gaussian n x n matrices.
+
+    Convention: 10 n^3 flop per real matrix (Hessenberg + double-shift QR,
+    eigenvalues only). Parity against LAPACK dgeev on an evenly spaced sample,
+    including LAPACK's conjugate-pair convention; LAPACK dgeev over the host
+    cores on a bounded sample for comparison.
+    """
+    import torch
+
+    from oracle import lapack_oracle as lo
+    from tokura_zgeev_batched_gb300 import api
+
+    g = torch.Generator(device=dev)
+    g.manual_seed(SEED + 5)
+    A = torch.randn(batch, n, n, generator=g, device=dev, dtype=torch.float64)
+    wr = torch.empty(batch, n, dtype=torch.float64, device=dev)
+    wi = torch.empty_like(wr)
+    flag = torch.empty(batch, dtype=torch.int8, device=dev)
+    work = torch.empty(api.tokura_get_dgeev_workspacesize(n, batch), dtype=torch.uint8, device=dev)
+
+    def call():
+        st = api.tokura_dgeev_batched_gpu(h, n, batch, A.data_ptr(), wr.data_ptr(), wi.data_ptr(), work.data_ptr(),
+                                          flag.data_ptr(), stream.cuda_stream)
+        if st != 0:
+            raise RuntimeError(f"tokura_dgeev_batched_gpu returned {st}")
+
+    ms = time_ms(call, 3, stream)
+    rate = batch / (ms * 1e-3)
+    idx = torch.arange(0, batch, max(1, batch // 256), device=dev)[:256]
+    rep = lo.real_parity_report(A[idx].cpu().numpy(), wr[idx].cpu().numpy(), wi[idx].cpu().numpy(),
+                                flag[idx].cpu().numpy())
+    threads = lo.default_threads()
+    sample = A[: max(threads * 16, 64)].cpu().numpy()
+    _, _, _, t = lo.dgeev(sample, threads)
+    cpu_count = int(min(max(sample.shape[0] / max(t, 1e-6) * cpu_seconds, threads * 8), batch))
+    _, _, _, t = lo.dgeev(A[:cpu_count].cpu().numpy(), threads)
+    return {"n": n, "batch": batch, "ms": ms, "matrices_per_s": rate,
+            "fp64_frac_10n3": 10.0 * n ** 3 * rate / peak, "flagged": int((flag != 0).sum().item()),
+            "parity": {"checked": int(idx.numel()), "max_rel_err_fro": rep["max_rel_err"],
+                       "max_rel_err_fro_cond_le_1e3": rep["max_rel_err_well"], "cond_le_1e3": rep["well_conditioned"],
+                       "flag_mismatch": rep["flag_mismatch"], "conjugate_pairs_exact": rep["pairs_ok"]},
+            "cpu_lapack_dgeev": {"matrices_per_s": cpu_count / t, "threads": threads, "sample": cpu_count}}
+
+
 def measure_config4(h, dev, stream, peak, batch: int = 50000, orders=(16, 48)) -> dict:
     """Differentiable eigenvalues: 50,000 separated-spectrum matrices each at n=16 and n=48.
 
@@ -731,6 +776,11 @@ def run_ours(args):
         phase("config 4 done")
         config5 = measure_config5(h, dev, stream, peak)
         phase("config 5 done")
+    real = None
+    if not args.no_real:
+        real = measure_real(h, dev, stream, peak)
+        torch.cuda.empty_cache()
+        phase("real path done")
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -748,7 +798,7 @@ def run_ours(args):
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
             "gpu_launches": args.steps, "flagged": flagged, "parity_spot_check": parity, "sweep": sweep,
             "config1_n32_10000": config1, "ragged": ragged, "config4_backward": config4,
-            "config5_ragged_gd_graph": config5,
+            "config5_ragged_gd_graph": config5, "real_dgeev_n64": real,
         }
         print(json.dumps(out), flush=True)
     if dist is not None:
@@ -769,6 +819,8 @@ def run_only(args):
     stream = torch.cuda.current_stream(dev)
     if args.only == "ragged":
         out = measure_ragged(h, dev, stream, peak, batch=args.batch or 200000)
+    elif args.only == "real":
+        out = measure_real(h, dev, stream, peak, n=args.n, batch=args.batch or 65536, cpu_seconds=0.5)
     else:
         out = measure_config4(h, dev, stream, peak, batch=args.batch or 50000, orders=(args.n,))
     print(json.dumps({"only": args.only, "result": out}), flush=True)
@@ -786,7 +838,8 @@ def main():
     ap.add_argument("--no-check", action="store_true")
     ap.add_argument("--no-ragged", action="store_true")
     ap.add_argument("--no-grad", action="store_true")
-    ap.add_argument("--only", choices=["ragged", "backward"], default=None,
+    ap.add_argument("--no-real", action="store_true")
+    ap.add_argument("--only", choices=["ragged", "backward", "real"], default=None,
                     help="run one configuration alone (profiling cases); --batch sets its size")
     ap.add_argument("--n", type=int, default=N, help="matrix order of the timed workload (profiling cases)")
     ap.add_argument("--batch", type=int, default=0, help="matrices per GPU (default: 4 GiB of input)")

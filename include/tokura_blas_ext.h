@@ -30,9 +30,24 @@ TOKURA_API int tokuraSetSweepCap(tokurablas_t* handle, int cap);
  * gain accuracy. Returns 0, -1 NULL handle, -2 bad mode. */
 TOKURA_API int tokuraSetBalancing(tokurablas_t* handle, int mode);
 
+/* FP32 shift hints for later eigenvalue calls on this handle (plain,
+ * strided, pointer-array, complex64, host-buffer and workspace-free entry
+ * points; not the ragged one, whose single persistent launch has no phase
+ * boundary to hide the estimator behind): 1 (default) computes
+ * single-precision eigenvalue estimates in a
+ * separate, cheap kernel (one warp per matrix in shared memory) and lets the
+ * FP64 QR use the nearest unused estimate as the shift of the first sweep
+ * after each deflation, for n >= 12; 0 uses Wilkinson shifts only. Results
+ * keep the FP64 accuracy either way (the estimates only steer the
+ * iteration; they are not bitwise identical between the two modes). The
+ * estimates occupy 8n bytes per matrix of the workspace after the staging
+ * area, inside the reference's workspace formula. Returns 0, -1 NULL
+ * handle, -2 bad mode. */
+TOKURA_API int tokuraSetShiftHints(tokurablas_t* handle, int mode);
+
 /* Launch shape of the plain kernel for order n: lanes per matrix (1, 2, 4, 8;
  * 0 = choose from the batch size) and threads per block (32..256, multiple
- * of 32; 0 = 128). Replaces the reference's compile-time tables
+ * of 32; 0 = 64). Replaces the reference's compile-time tables
  * (include/tokura_zhseqr_parameters.h, tokura_zgeev_batched.cu:13-60).
  * Returns 0, -1 NULL handle, -2 n out of range, -3 bad lanes, -4 bad threads. */
 TOKURA_API int tokuraSetPlainConfig(tokurablas_t* handle, int n, int lanes_per_matrix, int threads_per_block);
@@ -44,7 +59,7 @@ TOKURA_API int tokuraGetPlainConfig(const tokurablas_t* handle, int n, int batch
 /* Autotuner (replaces the reference's build-time tuner,
  * src/TOKURA_ZHSEQR_BATCHED_GEHRD_TUNING_main.cu:89-227, and its generated
  * tables). For each order n in [n_min, n_max], times every plain-kernel shape
- * (lanes per matrix 1/2/4/8 x threads per block 64/128/256) on batch_count
+ * (lanes per matrix 1/2/4/8 x threads per block 32/64/128/256) on batch_count
  * seeded synthetic complex Gaussian matrices and stores the fastest in the
  * handle. Allocates its own scratch (cudaMalloc), synchronizes `stream`.
  * Returns 0; -1 NULL handle, -2 bad range, -6 batch_count <= 0,
@@ -223,7 +238,8 @@ TOKURA_API int tokuraSetRealConfig(tokurablas_t* handle, int n, int lanes_per_ma
  * memory. The staging area is a 32 MiB static device array in the library
  * (held by every GPU that loads it until exit), so 16*n*n*batch_count must be
  * <= tokura_zgeev_noalloc_max_bytes(): at most 512 matrices of order 64,
- * 2048 of order 32. The first call on a device looks up that array's device
+ * 2048 of order 32 (the shift hints of tokuraSetShiftHints are used when
+ * their 8*n*batch_count bytes also fit). The first call on a device looks up that array's device
  * address, so make it before any stream capture starts. All calls share the
  * array: calls that overlap on the GPU race and must be ordered by the
  * caller (e.g. one stream). A is not modified.

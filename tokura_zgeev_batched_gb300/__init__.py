@@ -7,6 +7,8 @@ adds torch-tensor wrappers.
 from .api import (  # noqa: F401
     MAX_MATRIX_SIZE,
     Handle,
+    cgeev_batched,
+    dgeev_batched,
     default_handle,
     exported_symbols,
     lib,
@@ -15,4 +17,9 @@ from .api import (  # noqa: F401
     tokuraCreate,
     tokuraDestroy,
     zgeev_batched,
+    zgeev_batched_host,
+    zgeev_pointers,
+    zgeev_ragged,
+    zgeev_strided,
+    zgeev_vectors,
 )

@@ -57,6 +57,7 @@ _SIGNATURES = {
                              [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
     "tokuraSaveTuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
     "tokuraSetBalancing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "tokuraSetShiftHints": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "tokura_zgeev_vectors_batched_gpu": (
         ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 7),
     "tokura_get_zgeev_vectors_workspacesize": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int]),
@@ -161,6 +162,10 @@ class Handle:
     def set_balancing(self, mode: int) -> int:
         """0 none, 1 permute, 2 scale, 3 both (LAPACK zgeev's default)."""
         return int(lib().tokuraSetBalancing(self.ptr, int(mode)))
+
+    def set_shift_hints(self, mode: int) -> int:
+        """1 (default): FP32 eigenvalue estimates steer the FP64 QR's first shifts; 0: Wilkinson only."""
+        return int(lib().tokuraSetShiftHints(self.ptr, int(mode)))
 
     def set_real_config(self, n: int, lanes: int, threads: int) -> int:
         return int(lib().tokuraSetRealConfig(self.ptr, int(n), int(lanes), int(threads)))

@@ -29,7 +29,9 @@ SOURCES = [
     "zgeev_plain.cu",
     "peak_probe.cu",
     "zgeev_noalloc.cu",
-    "zgeev_layouts.cu",
+    "zgeev_strided.cu",
+    "zgeev_pointer.cu",
+    "cgeev_batched.cu",
     "dgeev_batched.cu",
     "zgeev_ragged.cu",
     "tokura_tuner.cu",

@@ -50,7 +50,7 @@ __device__ __forceinline__ int stage_and_scale_real(const Src& src, const RMatVi
     const int top = emax - 1023;
     if (top > 60 || top < -60) shift = top;
   }
-  const double sc = shift != 0 ? pow2(-shift) : 1.0;
+  const double sc = shift == 0 ? 1.0 : (shift > 1022 ? 0.5 * pow2(-1022) : pow2(-shift));
   for (int e = G.rank; e < nn; e += L) M.p[e * M.rs] = src.load(e) * sc;
   G.sync();
   return shift;

@@ -26,6 +26,14 @@ extern "C" int tokuraCreate(tokurablas_t** handle) {
     return 1;
   }
   tzg::init_default_tuning(h);
+  // The estimator's second stream; without it calls run the estimator first on the caller's stream.
+  h->fj.mu = &h->fj_mutex;
+  if (cudaStreamCreateWithFlags(&h->fj.aux, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->fj.fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&h->fj.join, cudaEventDisableTiming) != cudaSuccess) {
+    cudaGetLastError();
+    h->fj.aux = nullptr;
+  }
   // A tuning file written by tokuraSaveTuning for this device is applied if named in the environment.
   if (const char* path = std::getenv("TOKURA_ZGEEV_TUNING_FILE")) tokuraLoadTuning(h, path);
   *handle = h;
@@ -38,6 +46,9 @@ extern "C" int tokuraDestroy(tokurablas_t* handle) {
     const bool switch_dev = cudaGetDevice(&prev) == cudaSuccess && prev != handle->device;
     if (switch_dev) cudaSetDevice(handle->device);
     handle->pipe.release();
+    if (handle->fj.aux) cudaStreamDestroy(handle->fj.aux);
+    if (handle->fj.fork) cudaEventDestroy(handle->fj.fork);
+    if (handle->fj.join) cudaEventDestroy(handle->fj.join);
     if (switch_dev) cudaSetDevice(prev);
   }
   delete handle;
@@ -66,7 +77,7 @@ extern "C" int tokura_zgeev_batched_gpu(tokurablas_t* handle, int n, int batch_c
   const cudaError_t err = tzg::launch_plain(cfg, n, batch_count, reinterpret_cast<const double2*>(A),
                                             reinterpret_cast<double2*>(eigenvalues),
                                             reinterpret_cast<double2*>(work), flag, itmax, cudastream,
-                                            handle->balance_mode);
+                                            handle->balance_mode, tzg::use_shift_hints(handle, n), &handle->fj);
   return err == cudaSuccess ? 0 : 1;
 }
 
@@ -231,5 +242,12 @@ extern "C" int tokuraSetBalancing(tokurablas_t* handle, int mode) {
   if (handle == nullptr) return -1;
   if (mode < 0 || mode > 3) return -2;
   handle->balance_mode = mode;
+  return 0;
+}
+
+extern "C" int tokuraSetShiftHints(tokurablas_t* handle, int mode) {
+  if (handle == nullptr) return -1;
+  if (mode < 0 || mode > 1) return -2;
+  handle->shift_hints = mode;
   return 0;
 }

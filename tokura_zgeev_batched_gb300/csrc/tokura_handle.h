@@ -31,8 +31,11 @@ struct tokurablas_t {
   tzg::PlainConfig real[65] = {};  // the same for the real (dgeev/sgeev) kernel
   int ragged_lanes = 0;  // lanes per matrix of the ragged solvers; 0 = chosen per launch
   int balance_mode = 0;  // balancing before the eigenvalue solves: 0 none (the reference's behaviour) .. 3 both
+  int shift_hints = 1;   // FP32 eigenvalue estimates as first shifts: 0 off, 1 on for n >= kShiftHintMinN
   tzg::HostPipeline pipe;  // host-buffer entry point state (guarded by pipe_mutex)
   std::mutex pipe_mutex;
+  tzg::ForkJoin fj;        // second stream + events for the FP32 estimator (created with the handle)
+  std::mutex fj_mutex;
 };
 
 namespace tzg {
@@ -77,6 +80,12 @@ inline PlainConfig real_config_for(const tokurablas_t* h, int n, int batch) {
   if (c.threads == 0) c.threads = 64;
   return c;
 }
+
+// Orders from which the FP32 estimator pays for itself (below it the FP64
+// QR needs few sweeps and the extra launch dominates).
+constexpr int kShiftHintMinN = 12;
+
+inline bool use_shift_hints(const tokurablas_t* h, int n) { return h->shift_hints != 0 && n >= kShiftHintMinN; }
 
 inline int lanes_for_batch(const tokurablas_t* h, long long batch) {
   const long long want_lanes = (long long)h->sm_count * 4 * 2 * 32;

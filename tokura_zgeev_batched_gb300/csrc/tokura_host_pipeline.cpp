@@ -53,12 +53,13 @@ static cudaError_t ensure(HostPipeline& P, int n, int chunk, int streams) {
   if (!P.done && (err = cudaEventCreateWithFlags(&P.done, cudaEventDisableTiming)) != cudaSuccess) return err;
   const size_t a = sizeof(double2) * (size_t)n * n * chunk;
   const size_t e = sizeof(double2) * (size_t)n * chunk;
+  const size_t w = a + e;  // staging plus the shift hints (the device call's workspace formula)
   // Buffers of every stream grow to the largest chunk seen; caps are per
   // stream so a later call with more streams allocates the new ones.
   for (int s = 0; s < streams; ++s) {
     if ((err = grow(&P.d_a[s], &P.cap_a[s], a)) != cudaSuccess) return err;
     if ((err = grow(&P.d_eig[s], &P.cap_eig[s], e)) != cudaSuccess) return err;
-    if ((err = grow(&P.d_work[s], &P.cap_work[s], a)) != cudaSuccess) return err;
+    if ((err = grow(&P.d_work[s], &P.cap_work[s], w)) != cudaSuccess) return err;
     if ((err = grow(reinterpret_cast<void**>(&P.d_flag[s]), &P.cap_flag[s], (size_t)chunk)) != cudaSuccess)
       return err;
   }
@@ -104,8 +105,8 @@ extern "C" TOKURA_API int tokura_zgeev_batched_host(tokurablas_t* handle, int n,
       return 1;
     const tzg::PlainConfig cfg = tzg::plain_config_for(handle, n, batch_count);  // chunks run side by side
     if (tzg::launch_plain(cfg, n, m, static_cast<const double2*>(P.d_a[s]), static_cast<double2*>(P.d_eig[s]),
-                          static_cast<double2*>(P.d_work[s]), P.d_flag[s], itmax, st, handle->balance_mode) !=
-        cudaSuccess)
+                          static_cast<double2*>(P.d_work[s]), P.d_flag[s], itmax, st, handle->balance_mode,
+                          tzg::use_shift_hints(handle, n), &handle->fj) != cudaSuccess)
       return 1;
     if (cudaMemcpyAsync(eigenvalues + first * n, P.d_eig[s], sizeof(double2) * (size_t)n * m,
                         cudaMemcpyDeviceToHost, st) != cudaSuccess ||

@@ -90,7 +90,7 @@ extern "C" TOKURA_API int tokuraAutotune(tokurablas_t* handle, int n_min, int n_
   DeviceBuffers b;
   if (cudaMalloc(&b.p[0], sizeof(double2) * nn * batch_count) != cudaSuccess ||
       cudaMalloc(&b.p[1], sizeof(double2) * (size_t)n_max * batch_count) != cudaSuccess ||
-      cudaMalloc(&b.p[2], sizeof(double2) * nn * batch_count) != cudaSuccess ||
+      cudaMalloc(&b.p[2], sizeof(double2) * (nn + (size_t)n_max) * batch_count) != cudaSuccess ||
       cudaMalloc(&b.p[3], (size_t)batch_count) != cudaSuccess)
     return 2;
   double2* A = static_cast<double2*>(b.p[0]);
@@ -110,7 +110,8 @@ extern "C" TOKURA_API int tokuraAutotune(tokurablas_t* handle, int n_min, int n_
         const PlainConfig cfg{kLanes[li], kThreads[ti]};
         cudaError_t err;
         const float ms = time_launches(stream, 2, [&]() {
-          return launch_plain(cfg, n, batch_count, A, eig, work, flag, default_itmax(n), stream);
+          return launch_plain(cfg, n, batch_count, A, eig, work, flag, default_itmax(n), stream, 0,
+                              use_shift_hints(handle, n), &handle->fj);
         }, &err);
         if (err != cudaSuccess) return 1;
         if (ms < best) {

@@ -331,7 +331,7 @@ __device__ int backward_matrix(const double2* __restrict__ src, const double2* _
   hessenberg<L>(V.T, G, V.vec, V.vs);
   G.sync();
   form_q<L>(V, G);
-  const double lam_scale = shift != 0 ? pow2(-shift) : 1.0;
+  const double lam_scale = shift == 0 ? 1.0 : (shift > 1022 ? 0.5 * pow2(-1022) : pow2(-shift));
   const int status = schur_qr<L>(V, G, lam, gbar, lam_scale, itmax);
   if (status != kConverged) {
     const double nan = __longlong_as_double(0x7ff8000000000000LL);

@@ -1,6 +1,8 @@
 // Host-side internals shared by the C-ABI layer and the kernel launchers.
 #pragma once
 
+#include <mutex>
+
 #include <cuda_runtime.h>
 #include <stddef.h>
 #include <stdint.h>
@@ -18,8 +20,23 @@ __host__ __device__ inline int default_itmax(int n) { return 30 * (n > 10 ? n : 
 
 // Launches the fused stage + Hessenberg + QR kernel on `stream`.
 // `work` must hold 16*n*n*batch bytes (tile-interleaved copy of A).
+// A second stream and two events for running the FP32 estimator beside the
+// FP64 Hessenberg phase (fork from the caller's stream, join before the QR
+// phase). The mutex serializes the enqueue sequences of concurrent callers
+// so each join waits on its own fork.
+struct ForkJoin {
+  cudaStream_t aux = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+  std::mutex* mu = nullptr;
+};
+
+// hints: FP32 eigenvalue estimates steer the QR's first shifts; work must then
+// hold 16n^2*batch + 8n*batch + 4*batch bytes (inside the reference's
+// 16n^2*batch + 16n*batch). With fj, the estimator runs on fj->aux while the
+// Hessenberg phase runs on `stream`; without, it runs first on `stream`.
 cudaError_t launch_plain(const PlainConfig& cfg, int n, int batch, const double2* A, double2* eig,
-                         double2* work, char* flag, int itmax, cudaStream_t stream, int balance = 0);
+                         double2* work, char* flag, int itmax, cudaStream_t stream, int balance = 0,
+                         bool hints = false, const ForkJoin* fj = nullptr);
 
 // Ragged (per-matrix n) path: workspace bytes and launcher (device-side planning + persistent solve).
 size_t ragged_workspace_bytes(int batch, long long total_elements);

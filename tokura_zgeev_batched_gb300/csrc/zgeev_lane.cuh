@@ -68,7 +68,7 @@ __device__ __forceinline__ int stage_and_scale(const Src& src, const MatView& M,
   if (shift == 0) {
     for (int e = G.rank; e < nn; e += L) M.p[e * M.rs] = src.load(e, n);
   } else {
-    const double sc = pow2(-shift);
+    const double sc = shift > 1022 ? 0.5 * pow2(-1022) : pow2(-shift);  // 2^-1023 is subnormal
     for (int e = G.rank; e < nn; e += L) {
       const double2 z = src.load(e, n);
       M.p[e * M.rs] = make_double2(z.x * sc, z.y * sc);
@@ -341,6 +341,27 @@ __device__ void hessenberg(const MatView& M, const Group<L>& G, double2* tau_out
   }
 }
 
+// Index of the unused estimate nearest to t (bit k of `used` marks estimate k
+// as used), or -1 if none is finite. The scan is FP32 and identical in every
+// lane of a group, so all lanes agree.
+__device__ __forceinline__ int nearest_estimate(const float2* __restrict__ est, int n, unsigned long long used,
+                                                double2 t) {
+  const float tx = (float)t.x, ty = (float)t.y;
+  float best = 3.0e38f;
+  int k_best = -1;
+  for (int k = 0; k < n; ++k) {
+    if ((used >> k) & 1ull) continue;
+    const float2 e = est[k];
+    const float dx = e.x - tx, dy = e.y - ty;
+    const float d2 = fmaf(dx, dx, dy * dy);
+    if (d2 < best) {
+      best = d2;
+      k_best = k;
+    }
+  }
+  return k_best;
+}
+
 // Deflation test for subdiagonal entry k (k >= 1) of the active block [lo, hi]:
 // negligible by the Ahues-Tisseur criterion (LAPACK Working Note 122), with
 // smlnum guarding underflow. `tol` is the relative threshold (ulp for the
@@ -373,7 +394,8 @@ __device__ __forceinline__ bool negligible_subdiag(const MatView& M, int k, int 
 // (times 2^shift). Returns kConverged or kNotConverged. The per-eigenvalue
 // sweep cap defaults to LAPACK's 30*max(10, n).
 template <int L, class Out = double2>
-__device__ int qr_eigenvalues(const MatView& M, const Group<L>& G, Out* __restrict__ eig_out, int shift, int itmax) {
+__device__ int qr_eigenvalues(const MatView& M, const Group<L>& G, Out* __restrict__ eig_out, int shift, int itmax,
+                              const float2* __restrict__ est = nullptr) {
   const int n = M.n;
   const int rs = M.rs;
   const int cs = n * rs;
@@ -384,6 +406,7 @@ __device__ int qr_eigenvalues(const MatView& M, const Group<L>& G, Out* __restri
   int lo = 0;      // top of the active block [lo, i]
   int its = 0;     // sweeps since the last deflation (LAPACK's per-eigenvalue cap)
   int kdefl = 0;   // sweeps since the last deflation, for ad hoc shifts
+  unsigned long long used = 0;  // estimates already matched to a deflated eigenvalue
   // One loop iteration = (deflations, then) one sweep. Lanes of a warp hold
   // different matrices; keeping them in lockstep per sweep rather than per
   // eigenvalue means a lane whose eigenvalue converged early goes straight
@@ -402,9 +425,13 @@ __device__ int qr_eigenvalues(const MatView& M, const Group<L>& G, Out* __restri
       }
       lo = G.imax(hit);
       if (lo < i) break;
-      if (G.rank == 0) {
+      {
         const double2 d = *M.at(i, i);
-        put_ev(eig_out + i, make_double2(d.x * unscale, d.y * unscale));
+        if (G.rank == 0) put_ev(eig_out + i, make_double2(d.x * unscale, d.y * unscale));
+        if (est != nullptr) {
+          const int k = nearest_estimate(est, n, used, d);
+          if (k >= 0) used |= 1ull << k;
+        }
       }
       i -= 1;
       lo = 0;
@@ -430,6 +457,13 @@ __device__ int qr_eigenvalues(const MatView& M, const Group<L>& G, Out* __restri
         sigma = make_double2(d.x + kExceptionalWeight * cabs1(*M.at(lo + 1, lo)), d.y);
       } else {
         sigma = wilkinson_shift(*M.at(i - 1, i - 1), *M.at(i - 1, i), *M.at(i, i - 1), *M.at(i, i));
+        if (est != nullptr && its == 1) {  // first sweep for this position: the nearest FP32 estimate
+          const int k = nearest_estimate(est, n, used, sigma);
+          if (k >= 0) {
+            const float2 e = est[k];
+            sigma = make_double2((double)e.x, (double)e.y);
+          }
+        }
       }
       // One implicit single-shift sweep over the active block [lo, i].
       for (int j = lo; j < i; ++j) {
@@ -482,11 +516,17 @@ __device__ int qr_eigenvalues(const MatView& M, const Group<L>& G, Out* __restri
 // Hessenberg reduction, QR, eigenvalue write-out. Returns the flag value.
 // kBalance selects the instantiation that runs balance() with balance_mode;
 // without it the balancing code is not compiled into the kernel at all.
+// First half of solve_matrix: staging, balancing, Hessenberg reduction.
+// Returns kPrepared with the pre-scaling exponent in `shift` when the QR is
+// still to run, or the final flag value (eigenvalues already written) for
+// non-finite and zero matrices.
+constexpr int kPrepared = -1;
+
 template <int L, bool kBalance = false, class Src = SrcContig, class Out = double2>
-__device__ __forceinline__ int solve_matrix(const Src& src, const MatView& M, const Group<L>& G,
-                                            Out* __restrict__ ev, int itmax, int balance_mode = kBalanceNone) {
+__device__ __forceinline__ int prepare_matrix(const Src& src, const MatView& M, const Group<L>& G,
+                                              Out* __restrict__ ev, int balance_mode, int& shift) {
   bool nonfinite, zero;
-  const int shift = stage_and_scale<L>(src, M, G, nonfinite, zero);
+  shift = stage_and_scale<L>(src, M, G, nonfinite, zero);
   if (nonfinite || zero) {
     const double v = nonfinite ? __longlong_as_double(0x7ff8000000000000LL) : 0.0;
     for (int i = G.rank; i < M.n; i += L) put_ev(ev + i, make_double2(v, v));
@@ -494,14 +534,25 @@ __device__ __forceinline__ int solve_matrix(const Src& src, const MatView& M, co
   }
   if (kBalance) balance<L>(M, G, balance_mode);
   hessenberg<L>(M, G);
-  return qr_eigenvalues<L>(M, G, ev, shift, itmax);
+  return kPrepared;
+}
+
+template <int L, bool kBalance = false, class Src = SrcContig, class Out = double2>
+__device__ __forceinline__ int solve_matrix(const Src& src, const MatView& M, const Group<L>& G,
+                                            Out* __restrict__ ev, int itmax, int balance_mode = kBalanceNone,
+                                            const float2* __restrict__ est = nullptr) {
+  int shift;
+  const int status = prepare_matrix<L, kBalance>(src, M, G, ev, balance_mode, shift);
+  if (status != kPrepared) return status;
+  return qr_eigenvalues<L>(M, G, ev, shift, itmax, est);
 }
 
 // Contiguous column-major double-complex source (the reference's layout).
 template <int L, bool kBalance = false>
 __device__ __forceinline__ int solve_matrix(const double2* __restrict__ src, const MatView& M, const Group<L>& G,
-                                            double2* __restrict__ ev, int itmax, int balance_mode = kBalanceNone) {
-  return solve_matrix<L, kBalance, SrcContig, double2>(SrcContig{src}, M, G, ev, itmax, balance_mode);
+                                            double2* __restrict__ ev, int itmax, int balance_mode = kBalanceNone,
+                                            const float2* __restrict__ est = nullptr) {
+  return solve_matrix<L, kBalance, SrcContig, double2>(SrcContig{src}, M, G, ev, itmax, balance_mode, est);
 }
 
 }  // namespace tzg

@@ -11,7 +11,9 @@
 // file-scope __device__ array of kNoAllocScratchBytes (32 MiB), which every GPU
 // that loads this library keeps until the process exits. Calls with
 // 16*n*n*batch_count > 32 MiB are rejected with -8 (e.g. at most 512 matrices
-// of order 64, 2048 of order 32, 8192 of order 16).
+// of order 64, 2048 of order 32, 8192 of order 16). The FP32 shift hints
+// and the phase state (8n + 4 bytes per matrix) go behind the staging area
+// when they fit there; otherwise the call runs with Wilkinson shifts only.
 //
 // Host code must not hand the array's name to a kernel: on the host it is only
 // a stand-in symbol. The device address is obtained once per device, with that
@@ -71,6 +73,10 @@ extern "C" TOKURA_API int tokura_zgeev_batched_gpu_noalloc(tokurablas_t* handle,
   if (flag == nullptr) return -7;
   const size_t need = sizeof(double2) * (size_t)n * (size_t)n * (size_t)batch_count;
   if (need > tzg::kNoAllocScratchBytes) return -8;
+  // Shift hints only when they fit behind the staging area.
+  const bool hints = tzg::use_shift_hints(handle, n) &&
+                     need + (sizeof(float2) * (size_t)n + sizeof(int)) * (size_t)batch_count <=
+                         tzg::kNoAllocScratchBytes;
   double2* scratch = nullptr;
   if (tzg::noalloc_scratch_ptr(&scratch) != cudaSuccess) return 1;
   const tzg::PlainConfig cfg = tzg::plain_config_for(handle, n, batch_count);
@@ -78,6 +84,6 @@ extern "C" TOKURA_API int tokura_zgeev_batched_gpu_noalloc(tokurablas_t* handle,
   const cudaError_t err =
       tzg::launch_plain(cfg, n, batch_count, reinterpret_cast<const double2*>(A),
                         reinterpret_cast<double2*>(eigenvalues), scratch, flag, itmax, cudastream,
-                        handle->balance_mode);
+                        handle->balance_mode, hints, &handle->fj);
   return err == cudaSuccess ? 0 : 1;
 }
