@@ -26,8 +26,8 @@ def test_set_shift_hints_validation(cuda):
     from tokura_zgeev_batched_gb300 import api
 
     h = api.Handle()
-    assert h.set_shift_hints(0) == 0 and h.set_shift_hints(1) == 0
-    assert h.set_shift_hints(2) == -2 and h.set_shift_hints(-1) == -2
+    assert h.set_shift_hints(0) == 0 and h.set_shift_hints(1) == 0 and h.set_shift_hints(2) == 0
+    assert h.set_shift_hints(3) == -2 and h.set_shift_hints(-1) == -2
 
 
 @pytest.mark.parametrize("cls", ["gaussian", "vdv", "companion"])
@@ -128,3 +128,38 @@ def test_hints_on_every_layout_match_contiguous(cuda):
     torch.cuda.synchronize()
     assert torch.equal(w_s, w_c) and torch.equal(w_p, w_c)
     assert torch.equal(f_s, f_c) and torch.equal(f_p, f_c)
+
+
+@pytest.mark.parametrize("lanes", [0, 1, 4])
+def test_ragged_with_hints_everywhere(cuda, lanes):
+    """Mode 2 runs the ragged forward in two phases with the estimator beside
+    the first; parity with LAPACK and identical flags to mode 0."""
+    import torch
+    from tokura_zgeev_batched_gb300 import api
+
+    rng = np.random.default_rng(31)
+    mats = [wl.gaussian(1, int(n), seed=500 + k)[0] for k, n in enumerate(rng.integers(1, 65, size=240))]
+    mats[17] = np.zeros_like(mats[17])
+    mats[40] = mats[40].copy()
+    mats[40][0, 0] = np.inf
+    buf, ns, offs, eoffs = wl.pack_ragged([np.ascontiguousarray(m.T) for m in mats])
+    out = {}
+    for mode in (0, 2):
+        h = api.Handle()
+        assert h.set_shift_hints(mode) == 0 and h.set_ragged_lanes(lanes) == 0
+        eig, flag = api.zgeev_ragged(torch.from_numpy(buf).cuda(), torch.from_numpy(ns).cuda(), handle=h)
+        torch.cuda.synchronize()
+        out[mode] = (eig.cpu().numpy(), flag.cpu().numpy())
+    assert np.array_equal(out[0][1], out[2][1])
+    eig, flag = out[2]
+    assert flag[40] == 2 and flag[17] == 0 and (np.delete(flag, 40) == 0).all()
+    for k, m in enumerate(mats):
+        if k == 40:
+            continue
+        n = m.shape[0]
+        got = eig[eoffs[k]: eoffs[k] + n]
+        if k == 17:
+            assert (got == 0).all()
+            continue
+        w_ref = lo.zgeev(np.ascontiguousarray(m.T)[None])[0][0]
+        assert lo.matched_abs_errors(got, w_ref).max() <= lo.TOL_REL_FRO * np.linalg.norm(m), k

@@ -164,7 +164,8 @@ class Handle:
         return int(lib().tokuraSetBalancing(self.ptr, int(mode)))
 
     def set_shift_hints(self, mode: int) -> int:
-        """1 (default): FP32 eigenvalue estimates steer the FP64 QR's first shifts; 0: Wilkinson only."""
+        """FP32 eigenvalue estimates as first shifts: 1 (default) uniform batches with n >= 12,
+        2 every entry point and order (ragged too), 0 off (Wilkinson shifts only)."""
         return int(lib().tokuraSetShiftHints(self.ptr, int(mode)))
 
     def set_real_config(self, n: int, lanes: int, threads: int) -> int:

@@ -34,6 +34,7 @@ SOURCES = [
     "cgeev_batched.cu",
     "dgeev_batched.cu",
     "zgeev_ragged.cu",
+    "zgeev_ragged_split.cu",
     "tokura_tuner.cu",
     "zgeev_backward.cu",
     "zgeev_vectors.cu",

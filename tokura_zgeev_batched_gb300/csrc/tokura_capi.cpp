@@ -144,7 +144,8 @@ extern "C" int tokura_zgeev_ragged_gpu(tokurablas_t* handle, int batch_count, co
   const cudaError_t err = tzg::launch_ragged(handle->ragged_lanes, handle->sm_count, batch_count, n, offsets, eig_offsets,
                                              total_elements, reinterpret_cast<const double2*>(A),
                                              reinterpret_cast<double2*>(eigenvalues), work, flag,
-                                             handle->itmax_override, stream, handle->balance_mode);
+                                             handle->itmax_override, stream, handle->balance_mode,
+                                             tzg::use_ragged_shift_hints(handle), &handle->fj);
   return err == cudaSuccess ? 0 : 1;
 }
 
@@ -247,7 +248,7 @@ extern "C" int tokuraSetBalancing(tokurablas_t* handle, int mode) {
 
 extern "C" int tokuraSetShiftHints(tokurablas_t* handle, int mode) {
   if (handle == nullptr) return -1;
-  if (mode < 0 || mode > 1) return -2;
+  if (mode < 0 || mode > 2) return -2;
   handle->shift_hints = mode;
   return 0;
 }

@@ -31,7 +31,8 @@ struct tokurablas_t {
   tzg::PlainConfig real[65] = {};  // the same for the real (dgeev/sgeev) kernel
   int ragged_lanes = 0;  // lanes per matrix of the ragged solvers; 0 = chosen per launch
   int balance_mode = 0;  // balancing before the eigenvalue solves: 0 none (the reference's behaviour) .. 3 both
-  int shift_hints = 1;   // FP32 eigenvalue estimates as first shifts: 0 off, 1 on for n >= kShiftHintMinN
+  int shift_hints = 1;   // FP32 eigenvalue estimates as first shifts: 0 off, 1 uniform batches with
+                         // n >= kShiftHintMinN, 2 every eigenvalue entry point and order (ragged too)
   tzg::HostPipeline pipe;  // host-buffer entry point state (guarded by pipe_mutex)
   std::mutex pipe_mutex;
   tzg::ForkJoin fj;        // second stream + events for the FP32 estimator (created with the handle)
@@ -85,7 +86,15 @@ inline PlainConfig real_config_for(const tokurablas_t* h, int n, int batch) {
 // QR needs few sweeps and the extra launch dominates).
 constexpr int kShiftHintMinN = 12;
 
-inline bool use_shift_hints(const tokurablas_t* h, int n) { return h->shift_hints != 0 && n >= kShiftHintMinN; }
+inline bool use_shift_hints(const tokurablas_t* h, int n) {
+  return h->shift_hints == 2 || (h->shift_hints == 1 && n >= kShiftHintMinN);
+}
+
+// The ragged solver takes hints only when asked for everywhere: its
+// estimator (one pass over the whole batch, 225 ms for 200,000 orders in
+// U{1..64}) outlasts the Hessenberg phase it runs beside (157 ms), so with
+// hints the solve measured 690 ms against 670 ms without.
+inline bool use_ragged_shift_hints(const tokurablas_t* h) { return h->shift_hints == 2; }
 
 inline int lanes_for_batch(const tokurablas_t* h, long long batch) {
   const long long want_lanes = (long long)h->sm_count * 4 * 2 * 32;

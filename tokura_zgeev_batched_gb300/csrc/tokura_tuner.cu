@@ -151,7 +151,8 @@ extern "C" TOKURA_API int tokuraAutotuneRagged(tokurablas_t* handle, int batch_c
     cudaError_t err;
     const float ms = time_launches(stream, 2, [&]() {
       return launch_ragged(lanes, handle->sm_count, batch_count, n, off, nullptr, total, A,
-                           static_cast<double2*>(b.p[1]), b.p[2], static_cast<char*>(b.p[3]), 0, stream);
+                           static_cast<double2*>(b.p[1]), b.p[2], static_cast<char*>(b.p[3]), 0, stream, 0,
+                           use_ragged_shift_hints(handle), &handle->fj);
     }, &err);
     if (err != cudaSuccess) return 1;
     if (ms < best) {

@@ -516,6 +516,11 @@ __device__ int qr_eigenvalues(const MatView& M, const Group<L>& G, Out* __restri
 // Hessenberg reduction, QR, eigenvalue write-out. Returns the flag value.
 // kBalance selects the instantiation that runs balance() with balance_mode;
 // without it the balancing code is not compiled into the kernel at all.
+// Phases of a solve split in two launches (stage + Hessenberg, then QR), and
+// the per-matrix state value meaning "eigenvalues and flag already written".
+enum : int { kPhaseAll = 0, kPhasePrepare = 1, kPhaseQR = 2 };
+constexpr int kStateDone = -2147483647 - 1;
+
 // First half of solve_matrix: staging, balancing, Hessenberg reduction.
 // Returns kPrepared with the pre-scaling exponent in `shift` when the QR is
 // still to run, or the final flag value (eigenvalues already written) for

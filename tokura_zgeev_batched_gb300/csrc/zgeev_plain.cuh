@@ -28,8 +28,6 @@
 // depend on the split, so a given set of hints gives bitwise the same results.
 #pragma once
 
-#include <climits>
-
 #include "zgeev_estimate.cuh"
 #include "zgeev_internal.h"
 #include "zgeev_lane.cuh"
@@ -77,9 +75,6 @@ struct Complex64Batch {
   __device__ __forceinline__ SrcComplex64 src(long long j) const { return SrcComplex64{A + j * n * n}; }
   __device__ __forceinline__ float2* out(long long j, int) const { return W + j * n; }
 };
-
-enum : int { kPhaseAll = 0, kPhasePrepare = 1, kPhaseQR = 2 };
-constexpr int kStateDone = INT_MIN;  // phase state: eigenvalues and flag already written
 
 template <int L, bool kBalance, int kPhase, class Batch>
 __global__ void __launch_bounds__(256) zgeev_plain_kernel(int n, int batch, Batch B, double2* __restrict__ work,

@@ -18,54 +18,11 @@
 //               issued first so uneven QR iteration counts and sizes do not
 //               leave SMs idle at the end.
 #include <cmath>
+#include <mutex>
 
-#include "zgeev_backward.cuh"
-#include "zgeev_internal.h"
-#include "zgeev_lane.cuh"
+#include "zgeev_ragged.cuh"
 
 namespace tzg {
-
-struct RaggedBin {
-  int n;
-  int count;
-  int first;          // first position of this bin in sorted[]
-  int tile_start;     // first ticket of this bin
-  int tiles;
-  int lanes;          // lanes per matrix for this bin's tiles (1, 2, 4 or 8); a tile holds 32/lanes matrices
-  long long stage;    // first staging element of this bin
-};
-
-constexpr int kMaxQueues = 256;  // per-SM work queues (SM count of the device, at most this)
-
-struct RaggedPlan {
-  int hist[kMaxN + 1];
-  int cursor[kMaxN + 1];
-  RaggedBin bins[kMaxN];  // bins[b] holds n = 64 - b
-  int num_tiles;
-  int ticket;             // unused by the solvers; kept zero
-  int overflow;
-  int pad;
-  int queue[kMaxQueues];  // next position in each SM's share of the tiles
-};
-
-// Workspace layout (all sections 256-byte aligned).
-struct RaggedLayout {
-  size_t stage_off, plan_off, sorted_off, eoff_off, total;
-};
-
-static inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
-
-// `regions` staging areas of total_elements entries: 1 for the forward, 4 for
-// the backward (T, Q, XY and the per-matrix vectors).
-static RaggedLayout ragged_layout(int batch, long long total_elements, int regions = 1) {
-  RaggedLayout l;
-  l.stage_off = 0;
-  l.plan_off = align256(l.stage_off + sizeof(double2) * (size_t)total_elements * (size_t)regions);
-  l.sorted_off = align256(l.plan_off + sizeof(RaggedPlan));
-  l.eoff_off = align256(l.sorted_off + sizeof(int) * (size_t)batch);
-  l.total = align256(l.eoff_off + sizeof(long long) * (size_t)batch);
-  return l;
-}
 
 size_t ragged_workspace_bytes(int batch, long long total_elements) {
   return ragged_layout(batch, total_elements).total;
@@ -73,10 +30,6 @@ size_t ragged_workspace_bytes(int batch, long long total_elements) {
 
 size_t ragged_backward_workspace_bytes(int batch, long long total_elements) {
   return ragged_layout(batch, total_elements, 4).total;
-}
-
-__device__ __forceinline__ bool ragged_valid(int nj, long long off, long long total) {
-  return nj >= 1 && nj <= kMaxN && off >= 0 && off <= total - (long long)nj * nj;
 }
 
 __global__ void ragged_count_kernel(int batch, const int* __restrict__ n, const long long* __restrict__ offsets,
@@ -176,133 +129,6 @@ __global__ void __launch_bounds__(1024) ragged_scan_kernel(int batch, const int*
   }
 }
 
-// Ticket -> bin: largest b with bins[b].tile_start <= t (bins are in ticket order).
-__device__ __forceinline__ const RaggedBin& ragged_bin_of(const RaggedPlan* plan, int t) {
-  int lo = 0, hi = kMaxN - 1;
-  while (lo < hi) {
-    const int mid = (lo + hi + 1) >> 1;
-    if (plan->bins[mid].tile_start <= t) lo = mid; else hi = mid - 1;
-  }
-  return plan->bins[lo];
-}
-
-// Arguments of the ragged solvers.
-struct RaggedArgs {
-  const long long* offsets;
-  const long long* eoff;
-  const double2* A;
-  double2* eig;          // forward: eigenvalues out
-  const double2* lam;    // backward: forward eigenvalues
-  const double2* gbar;   // backward: their gradients
-  double2* gA;           // backward: gradient out
-  double2* stage;
-  long long region;      // backward: elements per staging region
-  char* flag;
-  const int* sorted;
-  int itmax_override;
-  int balance;           // forward: balancing mode
-};
-
-// Tile scheduling. Tiles are numbered in descending-work order; SM s owns
-// tiles s, s+Q, s+2Q, ... (Q queues, one per SM), i.e. an equal share of every
-// size class, and its warps take them in order through an atomic counter.
-// When its share is used up a warp takes tiles from the other SMs' shares.
-// Every atomicAdd returns a distinct position and a warp gives up after one
-// pass over all queues, so nothing waits on anything. Unlike a single global
-// ticket counter, the balance does not depend on the order in which blocks
-// reach the SMs.
-__device__ __forceinline__ unsigned sm_id() {
-  unsigned id;
-  asm volatile("mov.u32 %0, %%smid;" : "=r"(id));
-  return id;
-}
-
-__device__ __forceinline__ int ragged_next_tile(RaggedPlan* plan, int queues, int num_tiles, int& q) {
-  for (int tries = 0; tries < queues; ++tries) {
-    const int pos = atomicAdd(&plan->queue[q], 1);
-    const long long t = (long long)q + (long long)queues * pos;
-    if (t < num_tiles) return (int)t;
-    q = (q + 1 == queues) ? 0 : q + 1;  // this share is used up: move on to the next SM's share
-  }
-  return -1;
-}
-
-// Persistent solver with L lanes per matrix: takes tiles until all shares are
-// used up and solves (kBackward = false) or differentiates (true) each one;
-// kBalance (forward only) balances each matrix first with a.balance.
-// One instantiation per lane width, so each has its own register budget.
-template <int L, bool kBackward, bool kBalance = false>
-__global__ void __launch_bounds__(128) zgeev_ragged_kernel(RaggedPlan* plan, RaggedArgs a, int queues) {
-  constexpr int TW = 32 / L;
-  const int lane = threadIdx.x & 31;
-  const int slot = lane / L;
-  const int num_tiles = plan->num_tiles;
-  int q = (int)(sm_id() % (unsigned)queues);
-  for (;;) {
-    int t = 0;
-    if (lane == 0) t = ragged_next_tile(plan, queues, num_tiles, q);
-    t = __shfl_sync(0xffffffffu, t, 0);
-    if (t < 0) break;
-    const RaggedBin& bin = ragged_bin_of(plan, t);
-    const int u = t - bin.tile_start;
-    const int tw = min(TW, bin.count - u * TW);
-    if (slot < tw) {
-      const Group<L> G;
-      const int nb = bin.n;
-      const int j = a.sorted[bin.first + u * TW + slot];
-      const long long nn = (long long)nb * nb;
-      double2* base = a.stage + bin.stage + (long long)u * TW * nn + slot;
-      const int itmax = a.itmax_override > 0 ? a.itmax_override : default_itmax(nb);
-      int status;
-      if (kBackward) {
-        BwdViews V{MatView{base, nb, tw}, MatView{base + a.region, nb, tw}, MatView{base + 2 * a.region, nb, tw},
-                   base + 3 * a.region, tw};
-        status = backward_matrix<L>(a.A + a.offsets[j], a.lam + a.eoff[j], a.gbar + a.eoff[j],
-                                    a.gA + a.offsets[j], V, G, itmax);
-      } else {
-        status = solve_matrix<L, kBalance>(a.A + a.offsets[j], MatView{base, nb, tw}, G, a.eig + a.eoff[j], itmax,
-                                           a.balance);
-      }
-      if (G.rank == 0) a.flag[j] = (char)status;
-    }
-    __syncwarp();
-  }
-}
-
-template <typename Kernel>
-static int persistent_blocks(Kernel k, int sms) {
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, 128, 0) != cudaSuccess || per_sm < 1) per_sm = 1;
-  return sms * per_sm;
-}
-
-template <bool kBackward, bool kBalance = false>
-static cudaError_t launch_ragged_kernel(int lanes, int sms, RaggedPlan* plan, const RaggedArgs& args,
-                                        cudaStream_t stream) {
-  const int queues = sms < 1 ? 1 : (sms > kMaxQueues ? kMaxQueues : sms);
-  switch (lanes) {
-    case 1:
-      zgeev_ragged_kernel<1, kBackward, kBalance><<<persistent_blocks(zgeev_ragged_kernel<1, kBackward, kBalance>, sms),
-                                                    128, 0, stream>>>(plan, args, queues);
-      break;
-    case 2:
-      zgeev_ragged_kernel<2, kBackward, kBalance><<<persistent_blocks(zgeev_ragged_kernel<2, kBackward, kBalance>, sms),
-                                                    128, 0, stream>>>(plan, args, queues);
-      break;
-    case 4:
-      zgeev_ragged_kernel<4, kBackward, kBalance><<<persistent_blocks(zgeev_ragged_kernel<4, kBackward, kBalance>, sms),
-                                                    128, 0, stream>>>(plan, args, queues);
-      break;
-    case 8:
-      zgeev_ragged_kernel<8, kBackward, kBalance><<<persistent_blocks(zgeev_ragged_kernel<8, kBackward, kBalance>, sms),
-                                                    128, 0, stream>>>(plan, args, queues);
-      break;
-    default:
-      return cudaErrorInvalidValue;
-  }
-  return cudaGetLastError();
-}
-
 // Lane width of a ragged launch when the caller did not fix one: the smallest
 // L such that a tile of 32/L order-64 matrices (the worst case the host can
 // assume) stays below a third of the average work of an SM sub-partition,
@@ -345,21 +171,36 @@ static cudaError_t ragged_prepare(int lanes, int sms, int batch, const int* n, c
 
 cudaError_t launch_ragged(int lanes, int sms, int batch, const int* n, const long long* offsets,
                           const long long* eig_offsets, long long total_elements, const double2* A, double2* eig,
-                          void* work, char* flag, int itmax_override, cudaStream_t stream, int balance) {
+                          void* work, char* flag, int itmax_override, cudaStream_t stream, int balance, bool hints,
+                          const ForkJoin* fj) {
   if (lanes == 0) lanes = ragged_auto_lanes(sms, batch, total_elements);
   if (!(lanes == 1 || lanes == 2 || lanes == 4 || lanes == 8)) return cudaErrorInvalidValue;
   const RaggedLayout lay = ragged_layout(batch, total_elements);
-  double2* stage = reinterpret_cast<double2*>(static_cast<char*>(work) + lay.stage_off);
+  char* w = static_cast<char*>(work);
+  double2* stage = reinterpret_cast<double2*>(w + lay.stage_off);
+  float2* est = hints ? reinterpret_cast<float2*>(w + lay.est_off) : nullptr;
+  int* state = reinterpret_cast<int*>(w + lay.state_off);
+  const bool split = hints && fj != nullptr && fj->aux != nullptr;
+  std::unique_lock<std::mutex> lock;
+  cudaError_t err = cudaSuccess;
+  if (split) {  // the estimator starts first, beside the planning and the prepare phase
+    lock = std::unique_lock<std::mutex>(*fj->mu);
+    err = ragged_fork_estimates(sms, batch, n, offsets, total_elements, A, est, stream, *fj);
+  } else if (hints) {
+    err = launch_ragged_estimates(sms, batch, n, offsets, total_elements, A, est, stream);
+  }
+  if (err != cudaSuccess) return err;
   RaggedPlan* plan;
   int* sorted;
   const long long* eo;
-  cudaError_t err = ragged_prepare(lanes, sms, batch, n, offsets, eig_offsets, total_elements, lay, work, flag,
-                                   stream, &plan, &sorted, &eo);
+  err = ragged_prepare(lanes, sms, batch, n, offsets, eig_offsets, total_elements, lay, work, flag, stream, &plan,
+                       &sorted, &eo);
   if (err != cudaSuccess) return err;
   const RaggedArgs args{offsets, eo, A, eig, nullptr, nullptr, nullptr, stage, total_elements, flag, sorted,
-                        itmax_override, balance};
-  if (balance != 0) return launch_ragged_kernel<false, true>(lanes, sms, plan, args, stream);
-  return launch_ragged_kernel<false>(lanes, sms, plan, args, stream);
+                        itmax_override, balance, est, state};
+  if (split) return ragged_launch_phases(lanes, sms, plan, args, balance != 0, stream, *fj);
+  if (balance != 0) return launch_ragged_kernel<false, true, kPhaseAll>(lanes, sms, plan, args, stream);
+  return launch_ragged_kernel<false, false, kPhaseAll>(lanes, sms, plan, args, stream);
 }
 
 cudaError_t launch_ragged_backward(int lanes, int sms, int batch, const int* n, const long long* offsets,
@@ -377,8 +218,8 @@ cudaError_t launch_ragged_backward(int lanes, int sms, int batch, const int* n, 
                                    stream, &plan, &sorted, &eo);
   if (err != cudaSuccess) return err;
   const RaggedArgs args{offsets, eo, A, nullptr, lam, gbar, gA, stage, total_elements, flag, sorted, itmax_override,
-                        0};
-  return launch_ragged_kernel<true>(lanes, sms, plan, args, stream);
+                        0, nullptr, nullptr};
+  return launch_ragged_kernel<true, false, kPhaseAll>(lanes, sms, plan, args, stream);
 }
 
 }  // namespace tzg
