@@ -132,6 +132,7 @@ def test_create_destroy_null(lib):
     assert lib.tokuraDestroy(None) == 0
     assert lib.tokuraSetSweepCap(None, 3) == -1
     assert lib.tokuraSetBalancing(None, 3) == -1
+    assert lib.tokuraSetShiftHints(None, 1) == -1
 
 
 def test_reference_style_caller_links(tmp_path, lib):

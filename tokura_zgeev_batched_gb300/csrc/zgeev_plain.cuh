@@ -23,7 +23,10 @@
 // and the two ran one after the other: 790 -> 680 ms at n = 64 with the
 // largest carveout; smaller carveouts or an estimator grid capped to leave
 // registers for the prepare grid measured slower). The QR phase starts once both are
-// done. Between the phases each matrix's pre-scaling exponent (or a finished
+// done. The QR kernel asks for the same carveout (it measured indifferent to
+// it), so that when several calls run side by side (the host-buffer
+// pipeline's chunks) one call's QR blocks do not lock another call's
+// estimator out of an SM. Between the phases each matrix's pre-scaling exponent (or a finished
 // status) is kept in the workspace after the hints. The arithmetic does not
 // depend on the split, so a given set of hints gives bitwise the same results.
 #pragma once
@@ -125,7 +128,7 @@ template <int L, bool kBalance, int kPhase, class Batch>
 inline cudaError_t launch_plain_l(unsigned blocks, int threads, cudaStream_t stream, int n, int batch,
                                   const Batch& B, double2* work, char* flag, int itmax, int balance,
                                   const float2* est, int* state, int carveout) {
-  if (kPhase == kPhasePrepare) {  // shared memory for the estimator running beside it
+  if (kPhase != kPhaseAll) {  // shared memory for estimators running beside (this or another call's)
     const cudaError_t err = cudaFuncSetAttribute(zgeev_plain_kernel<L, kBalance, kPhase, Batch>,
                                                  cudaFuncAttributePreferredSharedMemoryCarveout, carveout);
     if (err != cudaSuccess) return err;
@@ -207,7 +210,7 @@ cudaError_t launch_batch(const PlainConfig& cfg, int n, int batch, const Batch& 
     return err;
   if ((err = cudaStreamWaitEvent(stream, fj->join, 0)) != cudaSuccess) return err;
   return launch_plain_phase<kPhaseQR>(L, false, (unsigned)blocks, threads, stream, n, batch, B, work, flag, itmax, 0,
-                                      est, state);
+                                      est, state, cudaSharedmemCarveoutMaxShared);
 }
 
 }  // namespace tzg

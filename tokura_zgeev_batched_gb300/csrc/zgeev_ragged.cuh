@@ -180,7 +180,7 @@ inline int persistent_blocks(Kernel k, int sms) {
 template <int L, bool kBackward, bool kBalance, int kPhase>
 inline cudaError_t launch_ragged_l(int sms, RaggedPlan* plan, const RaggedArgs& args, cudaStream_t stream) {
   const auto k = zgeev_ragged_kernel<L, kBackward, kBalance, kPhase>;
-  if (kPhase == kPhasePrepare) {  // shared memory for the FP32 estimator running beside it
+  if (kPhase != kPhaseAll) {  // shared memory for the FP32 estimator running beside it
     const cudaError_t err =
         cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
     if (err != cudaSuccess) return err;
