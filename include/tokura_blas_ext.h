@@ -48,7 +48,7 @@ TOKURA_API int tokuraSetShiftHints(tokurablas_t* handle, int mode);
 
 /* Launch shape of the plain kernel for order n: lanes per matrix (1, 2, 4, 8;
  * 0 = choose from the batch size) and threads per block (32..256, multiple
- * of 32; 0 = 64). Replaces the reference's compile-time tables
+ * of 32; 0 = 32). Replaces the reference's compile-time tables
  * (include/tokura_zhseqr_parameters.h, tokura_zgeev_batched.cu:13-60).
  * Returns 0, -1 NULL handle, -2 n out of range, -3 bad lanes, -4 bad threads. */
 TOKURA_API int tokuraSetPlainConfig(tokurablas_t* handle, int n, int lanes_per_matrix, int threads_per_block);

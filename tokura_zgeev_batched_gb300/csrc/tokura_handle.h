@@ -49,10 +49,12 @@ inline void init_default_tuning(tokurablas_t* h) {
 // Lanes per matrix: enough lane groups to give every SM sub-partition at
 // least two warps (FP64 saturates at one warp per sub-partition; the second
 // hides memory latency); otherwise spread each matrix over more lanes.
-// Blocks of 64 threads: when the whole batch is resident at once, the block
-// is the unit the hardware spreads over the SMs, so small blocks even out
-// the per-SM load (at n = 64, 65536 matrices: 2048 warps over 152 SMs run
-// about 11 % faster in 64-thread blocks than in 128-thread blocks).
+// One-warp blocks: when the whole batch is resident at once, the block is
+// the unit the hardware spreads over the SMs, so small blocks even out the
+// per-SM load (at n = 64, 65536 matrices: 2048 warps over 152 SMs run about
+// 11 % faster in 32- or 64-thread blocks than in 128-thread blocks; with
+// shift hints, 32-thread blocks are 5-9 % faster than 64 at batches of
+// 8,000-20,000 and equal at 65,536).
 inline PlainConfig plain_config_for(const tokurablas_t* h, int n, int batch) {
   PlainConfig c = h->plain[n];
   if (c.lanes == 0) {
@@ -65,7 +67,7 @@ inline PlainConfig plain_config_for(const tokurablas_t* h, int n, int batch) {
       c.lanes = 4;
     if (n <= 2) c.lanes = 1;
   }
-  if (c.threads == 0) c.threads = 64;
+  if (c.threads == 0) c.threads = 32;
   return c;
 }
 

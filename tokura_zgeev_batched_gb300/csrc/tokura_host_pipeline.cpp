@@ -79,12 +79,14 @@ extern "C" TOKURA_API int tokura_zgeev_batched_host(tokurablas_t* handle, int n,
   if (flag == nullptr) return -7;
   if (chunk_matrices < 0) return -8;
   using tzg::HostPipeline;
-  // Default: 8 chunks (at least 1024 matrices each). Every chunk in flight
+  // Default: 4 chunks (at least 1024 matrices each). Every chunk in flight
   // has its own stream and buffers (up to 16), so all chunk kernels can be
-  // resident together while later chunks are still being copied in.
+  // resident together while later chunks are still being copied in. (At
+  // n = 64 x 65,536 with 211 GB/s host copies: 4 chunks 709 ms, 8 chunks
+  // 734 ms, 16 chunks 808 ms, against 686 ms for the device-resident call.)
   int chunk = chunk_matrices;
   if (chunk == 0) {
-    chunk = (batch_count + 7) / 8;
+    chunk = (batch_count + 3) / 4;
     if (chunk < 1024) chunk = 1024;
   }
   if (chunk > batch_count) chunk = batch_count;
