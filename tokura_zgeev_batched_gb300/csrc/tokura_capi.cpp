@@ -217,7 +217,7 @@ extern "C" int tokura_zgeev_ragged_backward_gpu(tokurablas_t* handle, int batch_
 extern "C" size_t tokura_get_zgeev_vectors_workspacesize(int n, int batch_count) {
   if (!(0 < n && n <= TOKURA_ZGEEV_BATCHED_MAX_MATRIX_SIZE)) return (size_t)-1;
   if (!(0 < batch_count)) return (size_t)-2;
-  return tzg::backward_workspace_bytes(n, batch_count);
+  return tzg::vectors_workspace_bytes(n, batch_count);
 }
 
 extern "C" int tokura_zgeev_vectors_batched_gpu(tokurablas_t* handle, int n, int batch_count,
@@ -235,7 +235,8 @@ extern "C" int tokura_zgeev_vectors_batched_gpu(tokurablas_t* handle, int n, int
   const int itmax = handle->itmax_override > 0 ? handle->itmax_override : tzg::default_itmax(n);
   const cudaError_t err = tzg::launch_vectors(
       lanes, n, batch_count, reinterpret_cast<const double2*>(A), reinterpret_cast<double2*>(eigenvalues),
-      reinterpret_cast<double2*>(VL), reinterpret_cast<double2*>(VR), static_cast<double2*>(work), flag, itmax, stream);
+      reinterpret_cast<double2*>(VL), reinterpret_cast<double2*>(VR), static_cast<double2*>(work), flag, itmax, stream,
+      tzg::use_shift_hints(handle, n));
   return err == cudaSuccess ? 0 : 1;
 }
 

@@ -98,7 +98,8 @@ __device__ __forceinline__ int nearest_unused(const double2* __restrict__ lam, i
 // (lam == nullptr): Wilkinson/ad hoc shifts and the forward's ulp-level test.
 template <int L>
 __device__ int schur_qr(const BwdViews& V, const Group<L>& G, const double2* __restrict__ lam,
-                        const double2* __restrict__ gbar, double lam_scale, int itmax) {
+                        const double2* __restrict__ gbar, double lam_scale, int itmax,
+                        const float2* __restrict__ est = nullptr) {
   const double tol = lam != nullptr ? kGradDeflationTol : kUlp;
   const MatView& T = V.T;
   const MatView& Q = V.Q;
@@ -122,6 +123,9 @@ __device__ int schur_qr(const BwdViews& V, const Group<L>& G, const double2* __r
         const int kb = nearest_unused(lam, n, used, *T.at(i, i), lam_scale);
         used |= 1ull << kb;
         if (G.rank == 0) V.vec[i * V.vs] = gbar[kb];
+      } else if (est != nullptr) {
+        const int kb = nearest_estimate(est, n, used, *T.at(i, i));
+        if (kb >= 0) used |= 1ull << kb;
       }
       i -= 1;
       lo = 0;
@@ -136,10 +140,14 @@ __device__ int schur_qr(const BwdViews& V, const Group<L>& G, const double2* __r
     }
     double2 sigma;
     const double2 wk = wilkinson_shift(*T.at(i - 1, i - 1), *T.at(i - 1, i), *T.at(i, i - 1), *T.at(i, i));
+    int kb_est;
     if (its == 0 && lam != nullptr) {
       const double2 l = lam[nearest_unused(lam, n, used, wk, lam_scale)];
       sigma = make_double2(l.x * lam_scale, l.y * lam_scale);
       if (!(isfinite(sigma.x) && isfinite(sigma.y))) sigma = wk;
+    } else if (its == 0 && est != nullptr && (kb_est = nearest_estimate(est, n, used, wk)) >= 0) {
+      const float2 e = est[kb_est];  // FP32 shift hint (see zgeev_estimate.cuh)
+      sigma = make_double2((double)e.x, (double)e.y);
     } else if ((kdefl + 1) % (2 * kExceptionalPeriod) == 0) {
       const double2 d = *T.at(i, i);
       sigma = make_double2(d.x + kExceptionalWeight * cabs1(*T.at(i, i - 1)), d.y);

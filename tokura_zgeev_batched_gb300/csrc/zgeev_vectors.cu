@@ -9,6 +9,7 @@
 // LAPACK zgeev: unit 2-norm, component of largest modulus real and positive.
 #include "zgeev_backward.cuh"
 #include "zgeev_internal.h"
+#include "zgeev_plain.cuh"
 
 namespace tzg {
 
@@ -51,7 +52,8 @@ __device__ void schur_vectors(const BwdViews& V, const Group<L>& G, double2* __r
 
 template <int L>
 __device__ int vectors_matrix(const double2* __restrict__ src, double2* __restrict__ w_out, double2* __restrict__ VL,
-                              double2* __restrict__ VR, const BwdViews& V, const Group<L>& G, int itmax) {
+                              double2* __restrict__ VR, const BwdViews& V, const Group<L>& G, int itmax,
+                              const float2* __restrict__ est) {
   const int n = V.T.n;
   bool nonfinite, zero;
   const int shift = stage_and_scale<L>(src, V.T, G, nonfinite, zero);
@@ -67,7 +69,7 @@ __device__ int vectors_matrix(const double2* __restrict__ src, double2* __restri
   hessenberg<L>(V.T, G, V.vec, V.vs);
   G.sync();
   form_q<L>(V, G);
-  const int status = schur_qr<L>(V, G, nullptr, nullptr, 1.0, itmax);
+  const int status = schur_qr<L>(V, G, nullptr, nullptr, 1.0, itmax, est);
   const double unscale = shift != 0 ? pow2(shift) : 1.0;
   for (int i = G.rank; i < n; i += L) {
     const double2 d = *V.T.at(i, i);
@@ -85,7 +87,8 @@ template <int L>
 __global__ void __launch_bounds__(128) zgeev_vectors_kernel(int n, int batch, const double2* __restrict__ A,
                                                             double2* __restrict__ w, double2* __restrict__ VL,
                                                             double2* __restrict__ VR, double2* __restrict__ work,
-                                                            char* __restrict__ flag, int itmax) {
+                                                            char* __restrict__ flag, int itmax,
+                                                            const float2* __restrict__ est) {
   constexpr int TW = 32 / L;
   const int lane = threadIdx.x & 31;
   const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -102,12 +105,25 @@ __global__ void __launch_bounds__(128) zgeev_vectors_kernel(int n, int batch, co
   BwdViews V{MatView{base, n, tw}, MatView{base + region, n, tw}, MatView{base + 2 * region, n, tw},
              work + 3 * region + g0 * n + slot, tw};
   const int status = vectors_matrix<L>(A + j * nn, w + j * n, VL ? VL + j * nn : nullptr, VR ? VR + j * nn : nullptr,
-                                       V, G, itmax);
+                                       V, G, itmax, est != nullptr ? est + j * n : nullptr);
   if (G.rank == 0) flag[j] = (char)status;
 }
 
+size_t vectors_workspace_bytes(int n, int batch) {
+  return backward_workspace_bytes(n, batch) + sizeof(float2) * (size_t)n * (size_t)batch;
+}
+
+// hints: the FP32 estimator runs first on `stream` (its eigenvalues steer the
+// first shift after each deflation of the Schur iteration, as in the
+// eigenvalue path); they go after the backward-sized workspace.
 cudaError_t launch_vectors(int lanes, int n, int batch, const double2* A, double2* w, double2* VL, double2* VR,
-                           double2* work, char* flag, int itmax, cudaStream_t stream) {
+                           double2* work, char* flag, int itmax, cudaStream_t stream, bool hints) {
+  float2* est = nullptr;
+  if (hints) {
+    est = reinterpret_cast<float2*>(reinterpret_cast<char*>(work) + backward_workspace_bytes(n, batch));
+    const cudaError_t err = launch_estimates(n, batch, ContigBatch{A, nullptr, n}, est, stream);
+    if (err != cudaSuccess) return err;
+  }
   const int tw = 32 / lanes;
   const long long warps = ((long long)batch + tw - 1) / tw;
   const int threads = 64;  // small blocks spread a resident batch evenly over the SMs
@@ -115,16 +131,16 @@ cudaError_t launch_vectors(int lanes, int n, int batch, const double2* A, double
   if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
   switch (lanes) {
     case 1:
-      zgeev_vectors_kernel<1><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, w, VL, VR, work, flag, itmax);
+      zgeev_vectors_kernel<1><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, w, VL, VR, work, flag, itmax, est);
       break;
     case 2:
-      zgeev_vectors_kernel<2><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, w, VL, VR, work, flag, itmax);
+      zgeev_vectors_kernel<2><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, w, VL, VR, work, flag, itmax, est);
       break;
     case 4:
-      zgeev_vectors_kernel<4><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, w, VL, VR, work, flag, itmax);
+      zgeev_vectors_kernel<4><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, w, VL, VR, work, flag, itmax, est);
       break;
     case 8:
-      zgeev_vectors_kernel<8><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, w, VL, VR, work, flag, itmax);
+      zgeev_vectors_kernel<8><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, w, VL, VR, work, flag, itmax, est);
       break;
     default:
       return cudaErrorInvalidValue;
