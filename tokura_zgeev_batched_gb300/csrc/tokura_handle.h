@@ -15,7 +15,6 @@ struct HostPipeline {
   void* d_work[kStreams] = {};
   char* d_flag[kStreams] = {};
   cudaStream_t stream[kStreams] = {};
-  cudaEvent_t done = nullptr;
   size_t cap_a[kStreams] = {}, cap_eig[kStreams] = {}, cap_work[kStreams] = {}, cap_flag[kStreams] = {};
   void release();
 };
@@ -98,11 +97,5 @@ inline bool use_shift_hints(const tokurablas_t* h, int n) {
 // hints the solve measured 690 ms against 670 ms without.
 inline bool use_ragged_shift_hints(const tokurablas_t* h) { return h->shift_hints == 2; }
 
-inline int lanes_for_batch(const tokurablas_t* h, long long batch) {
-  const long long want_lanes = (long long)h->sm_count * 4 * 2 * 32;
-  if (batch >= want_lanes) return 1;
-  if (batch * 2 >= want_lanes) return 2;
-  return 4;
-}
 
 }  // namespace tzg

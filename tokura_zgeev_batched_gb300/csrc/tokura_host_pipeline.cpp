@@ -29,8 +29,6 @@ void HostPipeline::release() {
     d_flag[s] = nullptr;
     stream[s] = nullptr;
   }
-  if (done) cudaEventDestroy(done);
-  done = nullptr;
   for (int s = 0; s < kStreams; ++s) cap_a[s] = cap_eig[s] = cap_work[s] = cap_flag[s] = 0;
 }
 
@@ -50,7 +48,6 @@ static cudaError_t ensure(HostPipeline& P, int n, int chunk, int streams) {
     if (!P.stream[s] && (err = cudaStreamCreateWithFlags(&P.stream[s], cudaStreamNonBlocking)) != cudaSuccess)
       return err;
   }
-  if (!P.done && (err = cudaEventCreateWithFlags(&P.done, cudaEventDisableTiming)) != cudaSuccess) return err;
   const size_t a = sizeof(double2) * (size_t)n * n * chunk;
   const size_t e = sizeof(double2) * (size_t)n * chunk;
   const size_t w = a + e;  // staging plus the shift hints (the device call's workspace formula)

@@ -83,7 +83,6 @@ __global__ void ragged_plan_kernel(RaggedPlan* plan, int sms, int fixed_lanes, l
   // Matrices may overlap in A; the staging area holds total elements only.
   plan->overflow = stage > total;
   plan->num_tiles = plan->overflow ? 0 : tiles;
-  plan->ticket = 0;
 }
 
 __global__ void ragged_scatter_kernel(int batch, const int* __restrict__ n, const long long* __restrict__ offsets,

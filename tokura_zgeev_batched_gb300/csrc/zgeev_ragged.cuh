@@ -28,9 +28,7 @@ struct RaggedPlan {
   int cursor[kMaxN + 1];
   RaggedBin bins[kMaxN];  // bins[b] holds n = 64 - b
   int num_tiles;
-  int ticket;             // unused by the solvers; kept zero
   int overflow;
-  int pad;
   int queue[kMaxQueues];     // next position in each SM's share of the tiles
   int queue_qr[kMaxQueues];  // the same for the QR phase of a split solve
 };
