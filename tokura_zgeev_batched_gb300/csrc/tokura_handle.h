@@ -79,7 +79,7 @@ inline PlainConfig real_config_for(const tokurablas_t* h, int n, int batch) {
     c.lanes = (long long)batch >= want_lanes ? 1 : ((long long)batch * 2 >= want_lanes ? 2 : 4);
     if (n <= 2) c.lanes = 1;
   }
-  if (c.threads == 0) c.threads = 64;
+  if (c.threads == 0) c.threads = 32;
   return c;
 }
 

@@ -2,14 +2,15 @@
 //
 // Execution model (GB300): FP64 runs at ~2 lane-FMAs per clock per SM and a
 // warp instruction costs the same whether 1 or 32 lanes are active. The
-// kernels therefore give every matrix to a small "lane group" of L = 1, 2 or
-// 4 lanes of one warp (32/L matrices per warp), so that all 32 lanes do
+// kernels therefore give every matrix to a small "lane group" of L = 1, 2, 4
+// or 8 lanes of one warp (32/L matrices per warp), so that all 32 lanes do
 // useful FP64 work, and they keep FP64 instruction count minimal:
 //   * Householder Hessenberg reduction with v[0] = 1 and a real tau
 //     (replaces tokura_zgehrd_MWB_kernel.cuh:51-287 of the reference),
 //   * single-shift complex QR with complex Givens rotations (12 FP64 ops per
-//     element pair), Wilkinson shifts, ad hoc shifts and the Ahues-Tisseur
-//     deflation test (replaces tokura_zhseqr_MWB_kernel.cuh:221-791).
+//     element pair), Wilkinson shifts (or FP32 estimates as first shifts,
+//     zgeev_estimate.cuh), ad hoc shifts and the Ahues-Tisseur deflation
+//     test (replaces tokura_zhseqr_MWB_kernel.cuh:221-791).
 //
 // Data layout: each warp owns one "tile" of up to 32/L matrices, staged
 // from the caller's column-major A into the caller's workspace in

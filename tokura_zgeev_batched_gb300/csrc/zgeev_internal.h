@@ -11,7 +11,7 @@ namespace tzg {
 
 // Launch shape of the plain (uniform-n) forward kernel for one n.
 struct PlainConfig {
-  int lanes;            // lanes per matrix: 1, 2 or 4
+  int lanes;            // lanes per matrix: 1, 2, 4 or 8
   int threads;          // threads per block (multiple of 32)
 };
 
