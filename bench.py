@@ -794,7 +794,8 @@ def run_ours(args):
     if rank == 0:
         out = {
             "metric": METRIC, "value": value, "unit": "matrices/s", "n_gpus": ws, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+            "warmup": args.warmup, "ms_per_step": ms_step, "ms_per_step_median": statistics.median(kern_ms),
+            "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c128 (f64)", "data": "synthetic",
             "config": {"workload": f"plain zgeev eigenvalues (tokura_zgeev_batched_gpu), n={N}, {BATCH} complex "
                                    f"Gaussian matrices per GPU (4 GiB), seed {SEED}",

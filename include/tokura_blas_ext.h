@@ -150,8 +150,9 @@ TOKURA_API size_t tokura_get_zgeev_ragged_backward_workspacesize(int batch_count
  * as LAPACK zgeev returns them. VL or VR may be NULL. flag: 0 converged,
  * 1 QR cap hit, 2 non-finite input. work:
  * tokura_get_zgeev_vectors_workspacesize(n, batch_count) bytes (48*n*n*batch
- * + 24*n*batch; the last 8*n*batch hold the FP32 shift hints of
- * tokuraSetShiftHints). Return codes as tokura_zgeev_batched_gpu. */
+ * + 24*n*batch + 4*batch; the last 8*n*batch + 4*batch hold the FP32 shift
+ * hints of tokuraSetShiftHints and the per-matrix state between the two
+ * kernels of a hinted call). Return codes as tokura_zgeev_batched_gpu. */
 TOKURA_API int tokura_zgeev_vectors_batched_gpu(tokurablas_t* handle, int n, int batch_count, const cuDoubleComplex* A,
                                                 cuDoubleComplex* eigenvalues, cuDoubleComplex* VL,
                                                 cuDoubleComplex* VR, void* work, char* flag, cudaStream_t stream);

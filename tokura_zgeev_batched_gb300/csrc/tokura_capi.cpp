@@ -236,7 +236,7 @@ extern "C" int tokura_zgeev_vectors_batched_gpu(tokurablas_t* handle, int n, int
   const cudaError_t err = tzg::launch_vectors(
       lanes, n, batch_count, reinterpret_cast<const double2*>(A), reinterpret_cast<double2*>(eigenvalues),
       reinterpret_cast<double2*>(VL), reinterpret_cast<double2*>(VR), static_cast<double2*>(work), flag, itmax, stream,
-      tzg::use_shift_hints(handle, n));
+      tzg::use_shift_hints(handle, n), &handle->fj);
   return err == cudaSuccess ? 0 : 1;
 }
 

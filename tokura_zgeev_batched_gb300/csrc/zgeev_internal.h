@@ -57,7 +57,8 @@ cudaError_t launch_ragged_backward(int lanes, int sms, int batch, const int* n, 
 
 // Eigenvalues with eigenvectors (workspace: backward_workspace_bytes).
 cudaError_t launch_vectors(int lanes, int n, int batch, const double2* A, double2* w, double2* VL, double2* VR,
-                           double2* work, char* flag, int itmax, cudaStream_t stream, bool hints = false);
+                           double2* work, char* flag, int itmax, cudaStream_t stream, bool hints = false,
+                           const ForkJoin* fj = nullptr);
 size_t vectors_workspace_bytes(int n, int batch);
 
 }  // namespace tzg

@@ -50,13 +50,15 @@ __device__ void schur_vectors(const BwdViews& V, const Group<L>& G, double2* __r
   }
 }
 
+// First half: stage, Hessenberg (tau kept), Q. Returns kPrepared with the
+// pre-scaling exponent in `shift`, or the flag of a non-finite matrix (whose
+// outputs are then written).
 template <int L>
-__device__ int vectors_matrix(const double2* __restrict__ src, double2* __restrict__ w_out, double2* __restrict__ VL,
-                              double2* __restrict__ VR, const BwdViews& V, const Group<L>& G, int itmax,
-                              const float2* __restrict__ est) {
+__device__ int vectors_prepare(const double2* __restrict__ src, double2* __restrict__ w_out, double2* __restrict__ VL,
+                               double2* __restrict__ VR, const BwdViews& V, const Group<L>& G, int& shift) {
   const int n = V.T.n;
   bool nonfinite, zero;
-  const int shift = stage_and_scale<L>(src, V.T, G, nonfinite, zero);
+  shift = stage_and_scale<L>(src, V.T, G, nonfinite, zero);
   if (nonfinite) {
     const double nan = __longlong_as_double(0x7ff8000000000000LL);
     for (int i = G.rank; i < n; i += L) w_out[i] = make_double2(nan, nan);
@@ -69,6 +71,15 @@ __device__ int vectors_matrix(const double2* __restrict__ src, double2* __restri
   hessenberg<L>(V.T, G, V.vec, V.vs);
   G.sync();
   form_q<L>(V, G);
+  return kPrepared;
+}
+
+// Second half: Schur form with Q, eigenvalues, eigenvectors.
+template <int L>
+__device__ int vectors_finish(double2* __restrict__ w_out, double2* __restrict__ VL, double2* __restrict__ VR,
+                              const BwdViews& V, const Group<L>& G, int itmax, int shift,
+                              const float2* __restrict__ est) {
+  const int n = V.T.n;
   const int status = schur_qr<L>(V, G, nullptr, nullptr, 1.0, itmax, est);
   const double unscale = shift != 0 ? pow2(shift) : 1.0;
   for (int i = G.rank; i < n; i += L) {
@@ -83,12 +94,15 @@ __device__ int vectors_matrix(const double2* __restrict__ src, double2* __restri
   return kConverged;
 }
 
-template <int L>
+// kPhaseAll: the whole computation; kPhasePrepare / kPhaseQR: the two halves
+// in separate launches (state[j]: pre-scaling exponent or kStateDone), so the
+// FP32 estimator can run beside the first.
+template <int L, int kPhase>
 __global__ void __launch_bounds__(128) zgeev_vectors_kernel(int n, int batch, const double2* __restrict__ A,
                                                             double2* __restrict__ w, double2* __restrict__ VL,
                                                             double2* __restrict__ VR, double2* __restrict__ work,
                                                             char* __restrict__ flag, int itmax,
-                                                            const float2* __restrict__ est) {
+                                                            const float2* __restrict__ est, int* __restrict__ state) {
   constexpr int TW = 32 / L;
   const int lane = threadIdx.x & 31;
   const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -104,48 +118,87 @@ __global__ void __launch_bounds__(128) zgeev_vectors_kernel(int n, int batch, co
   double2* base = work + g0 * nn + slot;
   BwdViews V{MatView{base, n, tw}, MatView{base + region, n, tw}, MatView{base + 2 * region, n, tw},
              work + 3 * region + g0 * n + slot, tw};
-  const int status = vectors_matrix<L>(A + j * nn, w + j * n, VL ? VL + j * nn : nullptr, VR ? VR + j * nn : nullptr,
-                                       V, G, itmax, est != nullptr ? est + j * n : nullptr);
+  double2* vl = VL ? VL + j * nn : nullptr;
+  double2* vr = VR ? VR + j * nn : nullptr;
+  const float2* e = est != nullptr ? est + j * n : nullptr;
+  int status;
+  if (kPhase == kPhaseQR) {
+    const int s = state[j];
+    if (s == kStateDone) return;  // group-uniform
+    status = vectors_finish<L>(w + j * n, vl, vr, V, G, itmax, s, e);
+  } else {
+    int shift;
+    status = vectors_prepare<L>(A + j * nn, w + j * n, vl, vr, V, G, shift);
+    if (kPhase == kPhasePrepare) {
+      if (G.rank == 0) state[j] = status == kPrepared ? shift : kStateDone;
+      if (status == kPrepared) return;
+    } else if (status == kPrepared) {
+      status = vectors_finish<L>(w + j * n, vl, vr, V, G, itmax, shift, e);
+    }
+  }
   if (G.rank == 0) flag[j] = (char)status;
 }
 
 size_t vectors_workspace_bytes(int n, int batch) {
-  return backward_workspace_bytes(n, batch) + sizeof(float2) * (size_t)n * (size_t)batch;
+  return backward_workspace_bytes(n, batch) + (sizeof(float2) * (size_t)n + sizeof(int)) * (size_t)batch;
 }
 
-// hints: the FP32 estimator runs first on `stream` (its eigenvalues steer the
-// first shift after each deflation of the Schur iteration, as in the
-// eigenvalue path); they go after the backward-sized workspace.
-cudaError_t launch_vectors(int lanes, int n, int batch, const double2* A, double2* w, double2* VL, double2* VR,
-                           double2* work, char* flag, int itmax, cudaStream_t stream, bool hints) {
-  float2* est = nullptr;
-  if (hints) {
-    est = reinterpret_cast<float2*>(reinterpret_cast<char*>(work) + backward_workspace_bytes(n, batch));
-    const cudaError_t err = launch_estimates(n, batch, ContigBatch{A, nullptr, n}, est, stream);
-    if (err != cudaSuccess) return err;
+template <int kPhase>
+static cudaError_t launch_vectors_phase(int lanes, unsigned blocks, int threads, cudaStream_t stream, int n,
+                                        int batch, const double2* A, double2* w, double2* VL, double2* VR,
+                                        double2* work, char* flag, int itmax, const float2* est, int* state) {
+  const auto launch = [&](auto k) -> cudaError_t {
+    if (kPhase != kPhaseAll) {  // shared memory for the estimator running beside
+      const cudaError_t err =
+          cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
+      if (err != cudaSuccess) return err;
+    }
+    k<<<blocks, threads, 0, stream>>>(n, batch, A, w, VL, VR, work, flag, itmax, est, state);
+    return cudaGetLastError();
+  };
+  switch (lanes) {
+    case 1: return launch(zgeev_vectors_kernel<1, kPhase>);
+    case 2: return launch(zgeev_vectors_kernel<2, kPhase>);
+    case 4: return launch(zgeev_vectors_kernel<4, kPhase>);
+    case 8: return launch(zgeev_vectors_kernel<8, kPhase>);
+    default: return cudaErrorInvalidValue;
   }
+}
+
+// hints: FP32 estimates steer the first shift after each deflation of the
+// Schur iteration, as in the eigenvalue path; they and the phase state go
+// after the backward-sized workspace. With fj the estimator runs on fj->aux
+// beside the first half (stage, Hessenberg, Q); without, first on `stream`.
+cudaError_t launch_vectors(int lanes, int n, int batch, const double2* A, double2* w, double2* VL, double2* VR,
+                           double2* work, char* flag, int itmax, cudaStream_t stream, bool hints, const ForkJoin* fj) {
   const int tw = 32 / lanes;
   const long long warps = ((long long)batch + tw - 1) / tw;
-  const int threads = 64;  // small blocks spread a resident batch evenly over the SMs
+  const int threads = 32;  // one-warp blocks spread a resident batch evenly over the SMs
   const long long blocks = (warps * 32 + threads - 1) / threads;
   if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
-  switch (lanes) {
-    case 1:
-      zgeev_vectors_kernel<1><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, w, VL, VR, work, flag, itmax, est);
-      break;
-    case 2:
-      zgeev_vectors_kernel<2><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, w, VL, VR, work, flag, itmax, est);
-      break;
-    case 4:
-      zgeev_vectors_kernel<4><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, w, VL, VR, work, flag, itmax, est);
-      break;
-    case 8:
-      zgeev_vectors_kernel<8><<<(unsigned)blocks, threads, 0, stream>>>(n, batch, A, w, VL, VR, work, flag, itmax, est);
-      break;
-    default:
-      return cudaErrorInvalidValue;
+  if (!hints)
+    return launch_vectors_phase<kPhaseAll>(lanes, (unsigned)blocks, threads, stream, n, batch, A, w, VL, VR, work,
+                                           flag, itmax, nullptr, nullptr);
+  float2* est = reinterpret_cast<float2*>(reinterpret_cast<char*>(work) + backward_workspace_bytes(n, batch));
+  int* state = reinterpret_cast<int*>(est + (size_t)n * batch);
+  const ContigBatch src{A, nullptr, n};
+  cudaError_t err;
+  if (fj == nullptr || fj->aux == nullptr) {
+    if ((err = launch_estimates(n, batch, src, est, stream)) != cudaSuccess) return err;
+    return launch_vectors_phase<kPhaseAll>(lanes, (unsigned)blocks, threads, stream, n, batch, A, w, VL, VR, work,
+                                           flag, itmax, est, nullptr);
   }
-  return cudaGetLastError();
+  std::lock_guard<std::mutex> lock(*fj->mu);
+  if ((err = cudaEventRecord(fj->fork, stream)) != cudaSuccess) return err;
+  if ((err = cudaStreamWaitEvent(fj->aux, fj->fork, 0)) != cudaSuccess) return err;
+  if ((err = launch_estimates(n, batch, src, est, fj->aux)) != cudaSuccess) return err;
+  if ((err = cudaEventRecord(fj->join, fj->aux)) != cudaSuccess) return err;
+  if ((err = launch_vectors_phase<kPhasePrepare>(lanes, (unsigned)blocks, threads, stream, n, batch, A, w, VL, VR,
+                                                 work, flag, itmax, nullptr, state)) != cudaSuccess)
+    return err;
+  if ((err = cudaStreamWaitEvent(stream, fj->join, 0)) != cudaSuccess) return err;
+  return launch_vectors_phase<kPhaseQR>(lanes, (unsigned)blocks, threads, stream, n, batch, A, w, VL, VR, work, flag,
+                                        itmax, est, state);
 }
 
 }  // namespace tzg
