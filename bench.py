@@ -314,6 +314,56 @@ def measure_real(h, dev, stream, peak, n: int = 64, batch: int = 65536, cpu_seco
             "cpu_lapack_dgeev": {"matrices_per_s": cpu_count / t, "threads": threads, "sample": cpu_count}}
 
 
+def measure_vectors(h, dev, stream, n: int = 64, batch: int = 16384, cpu_seconds: float = 2.0) -> dict:
+    """Eigenvalues with left and right eigenvectors (tokura_zgeev_vectors_batched_gpu) on complex
+    Gaussian matrices: matrices/s (raw C-ABI call on device buffers), residuals
+    ||A VR - VR diag(w)|| / ||A|| and ||VL^H A - diag(w) VL^H|| / ||A|| on a sample, and LAPACK
+    zgeev('V','V') over the host cores on a bounded sample for comparison."""
+    import torch
+
+    from oracle import lapack_oracle as lo
+    from tokura_zgeev_batched_gb300 import api, workloads
+
+    A = workloads.torch_gaussian(batch, n, seed=SEED + 9, device=str(dev))
+    w = torch.empty(batch, n, dtype=torch.complex128, device=dev)
+    VL = torch.empty(batch, n, n, dtype=torch.complex128, device=dev)
+    VR = torch.empty(batch, n, n, dtype=torch.complex128, device=dev)
+    flag = torch.empty(batch, dtype=torch.int8, device=dev)
+    work = torch.empty(api.tokura_get_zgeev_vectors_workspacesize(n, batch), dtype=torch.uint8, device=dev)
+
+    def call():
+        st = api.lib().tokura_zgeev_vectors_batched_gpu(h.value, n, batch, A.data_ptr(), w.data_ptr(), VL.data_ptr(),
+                                                        VR.data_ptr(), work.data_ptr(), flag.data_ptr(),
+                                                        stream.cuda_stream)
+        if st != 0:
+            raise RuntimeError(f"tokura_zgeev_vectors_batched_gpu returned {st}")
+
+    ms = time_ms(call, 3, stream)
+    k = 64
+    # Buffers are column-major per matrix: the row-major views are the transposes.
+    Ak = A[:k].transpose(-1, -2)
+    VRk = VR[:k].transpose(-1, -2)
+    VLk = VL[:k].transpose(-1, -2)
+    wk = w[:k]
+    nA = torch.linalg.matrix_norm(Ak)
+    res_r = torch.linalg.matrix_norm(Ak @ VRk - VRk * wk[:, None, :]) / nA
+    res_l = torch.linalg.matrix_norm(VLk.conj().transpose(-1, -2) @ Ak - wk[:, :, None] * VLk.conj().transpose(-1, -2)) / nA
+    threads = lo.default_threads()
+    sample = A[: max(threads * 4, 32)].cpu().numpy()
+    t0 = time.perf_counter()
+    lo.zgeev_vectors(sample, threads)
+    t = time.perf_counter() - t0
+    count = int(min(max(sample.shape[0] / max(t, 1e-6) * cpu_seconds, threads * 4), batch))
+    big = A[:count].cpu().numpy()
+    t0 = time.perf_counter()
+    lo.zgeev_vectors(big, threads)
+    t = time.perf_counter() - t0
+    return {"n": n, "batch": batch, "ms": ms, "matrices_per_s": batch / (ms * 1e-3),
+            "flagged": int((flag != 0).sum().item()), "max_residual_right": float(res_r.max()),
+            "max_residual_left": float(res_l.max()),
+            "cpu_lapack_zgeev_vv": {"matrices_per_s": count / t, "threads": threads, "sample": count}}
+
+
 def measure_config4(h, dev, stream, peak, batch: int = 50000, orders=(16, 48)) -> dict:
     """Differentiable eigenvalues: 50,000 separated-spectrum matrices each at n=16 and n=48.
 
@@ -786,6 +836,11 @@ def run_ours(args):
         real = measure_real(h, dev, stream, peak)
         torch.cuda.empty_cache()
         phase("real path done")
+    vectors = None
+    if not args.no_vectors:
+        vectors = measure_vectors(h, dev, stream)
+        torch.cuda.empty_cache()
+        phase("eigenvectors done")
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -806,7 +861,7 @@ def run_ours(args):
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
             "gpu_launches": args.steps * (3 if N >= SHIFT_HINT_MIN_N else 1), "flagged": flagged, "parity_spot_check": parity, "sweep": sweep,
             "config1_n32_10000": config1, "ragged": ragged, "config4_backward": config4,
-            "config5_ragged_gd_graph": config5, "real_dgeev_n64": real,
+            "config5_ragged_gd_graph": config5, "real_dgeev_n64": real, "eigenvectors_n64": vectors,
         }
         print(json.dumps(out), flush=True)
     if dist is not None:
@@ -829,6 +884,8 @@ def run_only(args):
         out = measure_ragged(h, dev, stream, peak, batch=args.batch or 200000)
     elif args.only == "real":
         out = measure_real(h, dev, stream, peak, n=args.n, batch=args.batch or 65536, cpu_seconds=0.5)
+    elif args.only == "vectors":
+        out = measure_vectors(h, dev, stream, n=args.n, batch=args.batch or 16384, cpu_seconds=0.5)
     else:
         out = measure_config4(h, dev, stream, peak, batch=args.batch or 50000, orders=(args.n,))
     print(json.dumps({"only": args.only, "result": out}), flush=True)
@@ -847,7 +904,8 @@ def main():
     ap.add_argument("--no-ragged", action="store_true")
     ap.add_argument("--no-grad", action="store_true")
     ap.add_argument("--no-real", action="store_true")
-    ap.add_argument("--only", choices=["ragged", "backward", "real"], default=None,
+    ap.add_argument("--no-vectors", action="store_true")
+    ap.add_argument("--only", choices=["ragged", "backward", "real", "vectors"], default=None,
                     help="run one configuration alone (profiling cases); --batch sets its size")
     ap.add_argument("--n", type=int, default=N, help="matrix order of the timed workload (profiling cases)")
     ap.add_argument("--batch", type=int, default=0, help="matrices per GPU (default: 4 GiB of input)")

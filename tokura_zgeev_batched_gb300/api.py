@@ -616,6 +616,10 @@ def zgeev_batched_host(A, handle: Handle | None = None, chunk_matrices: int = 0)
     return eig.reshape(*shape[:-2], n), flag.reshape(shape[:-2])
 
 
+def tokura_get_zgeev_vectors_workspacesize(n: int, batch_count: int) -> int:
+    return int(lib().tokura_get_zgeev_vectors_workspacesize(int(n), int(batch_count)))
+
+
 def zgeev_vectors(A, left: bool = True, right: bool = True, handle: Handle | None = None, stream=None):
     """Eigenvalues and eigenvectors of complex128 CUDA matrices ``A[..., n, n]`` (ZGEEV with 'V').
 
