@@ -11,6 +11,7 @@
 // should be pinned (cudaHostAlloc / cudaHostRegister) for the copies to
 // overlap; pageable memory works but the driver then stages each copy.
 #include <mutex>
+#include <vector>
 
 #include "../../include/tokura_blas_ext.h"
 #include "tokura_handle.h"
@@ -42,22 +43,19 @@ static cudaError_t grow(void** p, size_t* cap, size_t need) {
   return err;
 }
 
-static cudaError_t ensure(HostPipeline& P, int n, int chunk, int streams) {
+// Streams 0..streams-1 with device buffers for chunk[s] matrices each.
+static cudaError_t ensure(HostPipeline& P, int n, const std::vector<int>& chunk, int streams) {
   cudaError_t err;
   for (int s = 0; s < streams; ++s) {
     if (!P.stream[s] && (err = cudaStreamCreateWithFlags(&P.stream[s], cudaStreamNonBlocking)) != cudaSuccess)
       return err;
-  }
-  const size_t a = sizeof(double2) * (size_t)n * n * chunk;
-  const size_t e = sizeof(double2) * (size_t)n * chunk;
-  const size_t w = a + e;  // staging plus the shift hints (the device call's workspace formula)
-  // Buffers of every stream grow to the largest chunk seen; caps are per
-  // stream so a later call with more streams allocates the new ones.
-  for (int s = 0; s < streams; ++s) {
+    const size_t a = sizeof(double2) * (size_t)n * n * chunk[s];
+    const size_t e = sizeof(double2) * (size_t)n * chunk[s];
+    const size_t w = a + e;  // staging plus the shift hints (the device call's workspace formula)
     if ((err = grow(&P.d_a[s], &P.cap_a[s], a)) != cudaSuccess) return err;
     if ((err = grow(&P.d_eig[s], &P.cap_eig[s], e)) != cudaSuccess) return err;
     if ((err = grow(&P.d_work[s], &P.cap_work[s], w)) != cudaSuccess) return err;
-    if ((err = grow(reinterpret_cast<void**>(&P.d_flag[s]), &P.cap_flag[s], (size_t)chunk)) != cudaSuccess)
+    if ((err = grow(reinterpret_cast<void**>(&P.d_flag[s]), &P.cap_flag[s], (size_t)chunk[s])) != cudaSuccess)
       return err;
   }
   return cudaSuccess;
@@ -76,33 +74,46 @@ extern "C" TOKURA_API int tokura_zgeev_batched_host(tokurablas_t* handle, int n,
   if (flag == nullptr) return -7;
   if (chunk_matrices < 0) return -8;
   using tzg::HostPipeline;
-  // Default: 4 chunks (at least 1024 matrices each). Every chunk in flight
-  // has its own stream and buffers (up to 16), so all chunk kernels can be
-  // resident together while later chunks are still being copied in. (At
-  // n = 64 x 65,536 with 211 GB/s host copies: 4 chunks 709 ms, 8 chunks
-  // 734 ms, 16 chunks 808 ms, against 686 ms for the device-resident call.)
-  int chunk = chunk_matrices;
-  if (chunk == 0) {
-    chunk = (batch_count + 3) / 4;
-    if (chunk < 1024) chunk = 1024;
+  // Chunk plan. Default: growing chunks of 1/16, 1/16, 1/8, 1/4, 1/2 of the
+  // batch (at least 1,024 matrices each), one stream and buffer set per chunk:
+  // the first solve starts after a small copy, and by the time the largest
+  // chunk has arrived the earlier ones have kept the GPU busy. With
+  // chunk_matrices > 0: equal chunks of that size, round-robin over up to 16
+  // streams.
+  std::vector<int> sizes;
+  if (chunk_matrices == 0) {
+    int c = (batch_count + 15) / 16;
+    if (c < 1024) c = 1024;
+    long long left = batch_count;
+    for (int k = 0; left > 0; ++k) {
+      const int want = k <= 1 ? c : (int)(sizes.back() * 2LL < left ? sizes.back() * 2LL : left);
+      const int m = (int)(want < left ? want : left);
+      sizes.push_back(m);
+      left -= m;
+    }
+  } else {
+    for (long long first = 0; first < batch_count; first += chunk_matrices)
+      sizes.push_back((int)(batch_count - first < chunk_matrices ? batch_count - first : chunk_matrices));
   }
-  if (chunk > batch_count) chunk = batch_count;
-  const long long chunks = (batch_count + (long long)chunk - 1) / chunk;
-  const int streams = chunks < HostPipeline::kStreams ? (int)chunks : HostPipeline::kStreams;
+  const int nchunks = (int)sizes.size();
+  const int streams = nchunks < HostPipeline::kStreams ? nchunks : HostPipeline::kStreams;
+  std::vector<int> cap(streams, 0);  // largest chunk each stream carries
+  for (int k = 0; k < nchunks; ++k) cap[k % streams] = sizes[k] > cap[k % streams] ? sizes[k] : cap[k % streams];
   std::lock_guard<std::mutex> lock(handle->pipe_mutex);
   HostPipeline& P = handle->pipe;
-  if (tzg::ensure(P, n, chunk, streams) != cudaSuccess) return 2;
+  if (tzg::ensure(P, n, cap, streams) != cudaSuccess) return 2;
   const int itmax = handle->itmax_override > 0 ? handle->itmax_override : tzg::default_itmax(n);
   const size_t nn = (size_t)n * n;
-  int k = 0;
-  for (long long first = 0; first < batch_count; first += chunk, ++k) {
+  // One launch shape for all chunks: they run side by side like one batch.
+  const tzg::PlainConfig cfg = tzg::plain_config_for(handle, n, batch_count);
+  long long first = 0;
+  for (int k = 0; k < nchunks; first += sizes[k], ++k) {
     const int s = k % streams;
-    const int m = (int)((batch_count - first) < chunk ? (batch_count - first) : chunk);
+    const int m = sizes[k];
     cudaStream_t st = P.stream[s];
     if (cudaMemcpyAsync(P.d_a[s], A + first * nn, sizeof(double2) * nn * m, cudaMemcpyHostToDevice, st) !=
         cudaSuccess)
       return 1;
-    const tzg::PlainConfig cfg = tzg::plain_config_for(handle, n, batch_count);  // chunks run side by side
     if (tzg::launch_plain(cfg, n, m, static_cast<const double2*>(P.d_a[s]), static_cast<double2*>(P.d_eig[s]),
                           static_cast<double2*>(P.d_work[s]), P.d_flag[s], itmax, st, handle->balance_mode,
                           tzg::use_shift_hints(handle, n), &handle->fj) != cudaSuccess)
