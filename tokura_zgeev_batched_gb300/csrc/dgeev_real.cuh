@@ -153,6 +153,33 @@ __device__ void hessenberg_real(const RMatView& M, const Group<L>& G) {
   G.sync();
 }
 
+// Applies the 3-element (NR = 3) or 2-element reflector of a double-shift
+// step, I - t1 [1 v2 v3]^T [1 v2 v3] (with t2 = t1 v2, t3 = t1 v3), to
+// `count` element triples p[t*step + {0, es, 2 es}]. Triple t+1 is loaded
+// before triple t is stored, so L1 latency overlaps the arithmetic.
+template <int NR>
+__device__ __forceinline__ void reflect_triples(double* p, int count, int step, int es, double v2, double v3,
+                                                double t1, double t2, double t3) {
+  if (count <= 0) return;
+  double a0 = p[0], a1 = p[es], a2 = NR == 3 ? p[2 * es] : 0.0;
+  for (int t = 1; t < count; ++t) {
+    double* pn = p + step;
+    const double b0 = pn[0], b1 = pn[es], b2 = NR == 3 ? pn[2 * es] : 0.0;
+    const double sum = NR == 3 ? fma(v3, a2, fma(v2, a1, a0)) : fma(v2, a1, a0);
+    p[0] = fma(-sum, t1, a0);
+    p[es] = fma(-sum, t2, a1);
+    if (NR == 3) p[2 * es] = fma(-sum, t3, a2);
+    a0 = b0;
+    a1 = b1;
+    a2 = b2;
+    p = pn;
+  }
+  const double sum = NR == 3 ? fma(v3, a2, fma(v2, a1, a0)) : fma(v2, a1, a0);
+  p[0] = fma(-sum, t1, a0);
+  p[es] = fma(-sum, t2, a1);
+  if (NR == 3) p[2 * es] = fma(-sum, t3, a2);
+}
+
 // Ahues-Tisseur test for subdiagonal k of the active block (dlahqr's).
 __device__ __forceinline__ bool negligible_real(const RMatView& M, int k, int n, double smlnum) {
   const double h = fabs(*M.at(k, k - 1));
@@ -433,40 +460,15 @@ __device__ int real_qr_eigenvalues(const RMatView& M, const Group<L>& G, Out* __
       }
       const double t2 = t1 * v2, t3 = t1 * v3;
       if (nr == 3) {
-        for (int j = k + G.rank; j <= i; j += L) {  // rows k..k+2, columns k..i
-          double* p = M.at(k, j);
-          const double a0 = p[0], a1 = p[rs], a2 = p[2 * rs];
-          const double sum = fma(v3, a2, fma(v2, a1, a0));
-          p[0] = fma(-sum, t1, a0);
-          p[rs] = fma(-sum, t2, a1);
-          p[2 * rs] = fma(-sum, t3, a2);
-        }
+        // rows k..k+2 of columns k..i, then columns k..k+2 of rows l..min(k+3, i)
+        reflect_triples<3>(M.at(k, k + G.rank), strided_count(k + G.rank, i, L), L * cs, rs, v2, v3, t1, t2, t3);
         G.sync();
-        const int jend = min(k + 3, i);
-        for (int j = l + G.rank; j <= jend; j += L) {  // columns k..k+2, rows l..min(k+3, i)
-          double* p = M.at(j, k);
-          const double a0 = p[0], a1 = p[cs], a2 = p[2 * cs];
-          const double sum = fma(v3, a2, fma(v2, a1, a0));
-          p[0] = fma(-sum, t1, a0);
-          p[cs] = fma(-sum, t2, a1);
-          p[2 * cs] = fma(-sum, t3, a2);
-        }
+        reflect_triples<3>(M.at(l + G.rank, k), strided_count(l + G.rank, min(k + 3, i), L), L * rs, cs, v2, v3, t1,
+                           t2, t3);
       } else {
-        for (int j = k + G.rank; j <= i; j += L) {
-          double* p = M.at(k, j);
-          const double a0 = p[0], a1 = p[rs];
-          const double sum = fma(v2, a1, a0);
-          p[0] = fma(-sum, t1, a0);
-          p[rs] = fma(-sum, t2, a1);
-        }
+        reflect_triples<2>(M.at(k, k + G.rank), strided_count(k + G.rank, i, L), L * cs, rs, v2, 0.0, t1, t2, 0.0);
         G.sync();
-        for (int j = l + G.rank; j <= i; j += L) {
-          double* p = M.at(j, k);
-          const double a0 = p[0], a1 = p[cs];
-          const double sum = fma(v2, a1, a0);
-          p[0] = fma(-sum, t1, a0);
-          p[cs] = fma(-sum, t2, a1);
-        }
+        reflect_triples<2>(M.at(l + G.rank, k), strided_count(l + G.rank, i, L), L * rs, cs, v2, 0.0, t1, t2, 0.0);
       }
       G.sync();
     }
