@@ -40,3 +40,21 @@ def test_host_entry_argument_codes(cuda):
     assert f(h, 2, 0, p, p, p) == -6
     assert f(h, 2, 1, p, p, None) == -7
     assert f(h, 2, 1, p, p, p, -1) == -8
+
+
+@pytest.mark.parametrize("batch", [3000, 10000, 40000])
+def test_host_entry_growing_chunks_bitwise_equal_device_call(cuda, batch):
+    """The default chunk plan (1/16, 1/16, 1/8, 1/4, 1/2 of the batch, each at
+    least 1,024 matrices) cuts the batch differently from the device call, but
+    every matrix is solved by the same arithmetic: bitwise the same results."""
+    import torch
+
+    n = 16
+    A = wl.torch_gaussian(batch, n, seed=batch)
+    w_dev, f_dev = api.zgeev_batched(A)
+    torch.cuda.synchronize()
+    # zgeev_batched reads the row-major tensor as column-major A^T; pass the same buffer.
+    A_host = A.cpu().pin_memory()
+    w_host, f_host = api.zgeev_batched_host(A_host)
+    assert np.array_equal(w_host.view(np.uint64), w_dev.cpu().numpy().view(np.uint64))
+    assert np.array_equal(f_host, f_dev.cpu().numpy())

@@ -75,3 +75,19 @@ def test_noalloc_rejects_batches_beyond_the_static_array(cuda):
                                                     ctypes.c_void_p(0))
     assert st == -8
     assert api.lib().tokura_zgeev_batched_gpu_noalloc(None, n, 1, A.data_ptr(), A.data_ptr(), A.data_ptr(), None) == -1
+
+
+def test_noalloc_with_and_without_room_for_shift_hints(cuda):
+    """At n = 64, 500 matrices leave room for the FP32 hints behind the staging
+    area and 512 do not: both calls succeed and match LAPACK."""
+    import torch
+
+    h = api.Handle()
+    stream = torch.cuda.current_stream().cuda_stream
+    for batch in (500, 512):
+        A_np = wl.gaussian(batch, 64, seed=batch)
+        A = torch.from_numpy(A_np).cuda()
+        e, f = noalloc(h, A, 64, batch, stream)
+        torch.cuda.synchronize()
+        rep = lo.parity_report(A_np, e.cpu().numpy(), f.cpu().numpy(), with_cond=False)
+        assert rep["flag_mismatch"] == 0 and rep["max_rel_err"] <= lo.TOL_REL_FRO
