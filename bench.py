@@ -264,9 +264,25 @@ def measure_config1(h, dev, stream, peak, call) -> dict:
     work = torch.empty(api.tokura_get_zgeeveigenvaluesgetworspacesize(n, batch), dtype=torch.uint8, device=dev)
     ms = time_ms(lambda: call(n, batch, A, eig, flag, work), 5, stream)
     rate = batch / (ms * 1e-3)
-    return {"n": n, "batch": batch, "ms": ms, "matrices_per_s": rate, "fp64_frac": flops_per_matrix(n) * rate / peak,
-            "lanes_per_matrix": h.plain_config(n, batch)[0], "flagged": int((flag != 0).sum().item()),
-            "parity": spot_check(A, eig, flag, 256)}
+    out = {"n": n, "batch": batch, "ms": ms, "matrices_per_s": rate, "fp64_frac": flops_per_matrix(n) * rate / peak,
+           "lanes_per_matrix": h.plain_config(n, batch)[0], "flagged": int((flag != 0).sum().item()),
+           "parity": spot_check(A, eig, flag, 256)}
+    # The same call on a handle tuned for this order and batch (tokuraAutotune).
+    ht = api.Handle()
+    if ht.autotune(n, n, batch, stream.cuda_stream) == 0:
+        def tuned_call():
+            st = api.tokura_zgeev_batched_gpu(ht, n, batch, A.data_ptr(), eig.data_ptr(), work.data_ptr(),
+                                              flag.data_ptr(), stream.cuda_stream)
+            if st != 0:
+                raise RuntimeError(f"tokura_zgeev_batched_gpu returned {st}")
+
+        ms_t = time_ms(tuned_call, 5, stream)
+        lanes, threads = ht.plain_config(n, batch)
+        out["autotuned"] = {"ms": ms_t, "matrices_per_s": batch / (ms_t * 1e-3),
+                            "fp64_frac": flops_per_matrix(n) * batch / (ms_t * 1e-3) / peak,
+                            "lanes_per_matrix": lanes, "threads_per_block": threads,
+                            "flagged": int((flag != 0).sum().item())}
+    return out
 
 
 def measure_real(h, dev, stream, peak, n: int = 64, batch: int = 65536, cpu_seconds: float = 2.0) -> dict:
@@ -886,6 +902,14 @@ def run_only(args):
         out = measure_real(h, dev, stream, peak, n=args.n, batch=args.batch or 65536, cpu_seconds=0.5)
     elif args.only == "vectors":
         out = measure_vectors(h, dev, stream, n=args.n, batch=args.batch or 16384, cpu_seconds=0.5)
+    elif args.only == "config1":
+        def call(n, batch, A, eig, flag, work):
+            st = api.tokura_zgeev_batched_gpu(h, n, batch, A.data_ptr(), eig.data_ptr(), work.data_ptr(),
+                                              flag.data_ptr(), stream.cuda_stream)
+            if st != 0:
+                raise RuntimeError(f"tokura_zgeev_batched_gpu returned {st}")
+
+        out = measure_config1(h, dev, stream, peak, call)
     else:
         out = measure_config4(h, dev, stream, peak, batch=args.batch or 50000, orders=(args.n,))
     print(json.dumps({"only": args.only, "result": out}), flush=True)
@@ -905,7 +929,7 @@ def main():
     ap.add_argument("--no-grad", action="store_true")
     ap.add_argument("--no-real", action="store_true")
     ap.add_argument("--no-vectors", action="store_true")
-    ap.add_argument("--only", choices=["ragged", "backward", "real", "vectors"], default=None,
+    ap.add_argument("--only", choices=["ragged", "backward", "real", "vectors", "config1"], default=None,
                     help="run one configuration alone (profiling cases); --batch sets its size")
     ap.add_argument("--n", type=int, default=N, help="matrix order of the timed workload (profiling cases)")
     ap.add_argument("--batch", type=int, default=0, help="matrices per GPU (default: 4 GiB of input)")

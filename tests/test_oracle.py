@@ -127,3 +127,69 @@ def test_reference_algorithm_real_part_deflation_quirk():
     assert flag[0] == 0 and info[0] == 0
     assert np.allclose(np.sort_complex(w[0]), [1, 4, 6])
     assert lo.matched_abs_errors(w, wr).max() > 0.1
+
+
+# ---- real path oracle (LAPACK dgeev via oracle/cpu_zgeev.c)
+
+def _rotation_blocks(n: int, rng) -> tuple[np.ndarray, np.ndarray]:
+    """Q^T B Q with B block diagonal: 2x2 blocks [[a, -b], [b, a]] (eigenvalues a +- ib)
+    and, for odd n, one 1x1 block. Returns (matrix, exact spectrum)."""
+    B = np.zeros((n, n))
+    lam = []
+    for k in range(0, n - 1, 2):
+        a, b = rng.uniform(-2, 2), rng.uniform(0.5, 2)
+        B[k:k + 2, k:k + 2] = [[a, -b], [b, a]]
+        lam += [a + 1j * b, a - 1j * b]
+    if n % 2:
+        B[-1, -1] = rng.uniform(-2, 2)
+        lam.append(B[-1, -1])
+    Q, _ = np.linalg.qr(rng.standard_normal((n, n)))
+    return Q.T @ B @ Q, np.array(lam)
+
+
+@pytest.mark.parametrize("n", [2, 5, 16, 33])
+def test_real_oracle_known_spectra(n):
+    rng = np.random.default_rng(100 + n)
+    mats, exact = zip(*[_rotation_blocks(n, rng) for _ in range(6)])
+    A = np.stack(mats)
+    wr, wi, info, _ = lo.dgeev(A, threads=2)
+    assert (info == 0).all()
+    assert lo.check_conjugate_pairs(wr, wi)
+    # Orthogonal similarity of normal blocks: eigenvalue condition numbers are 1.
+    err = lo.matched_abs_errors(wr + 1j * wi, np.stack(exact))
+    fro = np.linalg.norm(A, axis=(1, 2))
+    assert np.all(err.max(axis=1) <= 1e-13 * fro), err.max(axis=1) / fro
+
+
+def test_real_oracle_agrees_with_complex_oracle():
+    rng = np.random.default_rng(5)
+    A = rng.standard_normal((8, 12, 12))
+    wr, wi, info, _ = lo.dgeev(A, threads=2)
+    w, zinfo, _ = lo.zgeev(A.astype(np.complex128), threads=2)
+    assert (info == 0).all() and (zinfo == 0).all()
+    err = lo.matched_abs_errors(wr + 1j * wi, w)
+    assert err.max() <= 1e-12 * np.linalg.norm(A, axis=(1, 2)).max()
+
+
+def test_conjugate_pair_convention_checker():
+    wr = np.array([[1.0, 1.0, 3.0]])
+    assert lo.check_conjugate_pairs(wr, np.array([[2.0, -2.0, 0.0]]))
+    assert not lo.check_conjugate_pairs(wr, np.array([[-2.0, 2.0, 0.0]]))  # negative part first
+    assert not lo.check_conjugate_pairs(wr, np.array([[2.0, -2.0 + 1e-15, 0.0]]))  # not exact conjugates
+    assert not lo.check_conjugate_pairs(np.array([[1.0, 1.0 + 1e-15, 3.0]]), np.array([[2.0, -2.0, 0.0]]))
+    assert not lo.check_conjugate_pairs(wr, np.array([[0.0, 0.0, 2.0]]))  # pair cut off at the end
+
+
+def test_real_parity_report_detects_errors():
+    rng = np.random.default_rng(9)
+    A = rng.standard_normal((4, 7, 7))
+    wr, wi, _, _ = lo.dgeev(A, threads=2)
+    flags = np.zeros(4, np.int8)
+    rep = lo.real_parity_report(A, wr, wi, flags)
+    assert rep["max_rel_err"] < 1e-14 and rep["flag_mismatch"] == 0 and rep["pairs_ok"]
+    bad = wr.copy()
+    bad[1, 0] += 1e-6
+    rep = lo.real_parity_report(A, bad, wi, flags)
+    assert rep["max_rel_err"] > 1e-8
+    flags[3] = 1
+    assert lo.real_parity_report(A, wr, wi, flags)["flag_mismatch"] == 1
