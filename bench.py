@@ -763,11 +763,25 @@ def run_ours(args):
     # steps issued back to back on one stream are reported as "single_stream".
     e2e = None
     if not args.no_e2e:
-        A_host = torch.empty(A.shape, dtype=A.dtype, pin_memory=True)
+        # Pinned host buffers from the library's allocator (tokuraHostAlloc: huge pages, so the
+        # host link keeps its full rate after the idle gaps between steps).
+        A_host = api.host_empty(A.shape, A.dtype)
         A_host.copy_(A)
-        eig_host = torch.empty(eig.shape, dtype=eig.dtype, pin_memory=True)
-        flag_host = torch.empty(flag.shape, dtype=flag.dtype, pin_memory=True)
+        eig_host = api.host_empty(eig.shape, eig.dtype)
+        flag_host = api.host_empty(flag.shape, flag.dtype)
         torch.cuda.synchronize()
+
+        def h2d_rate():
+            """The host link's rate now (one pinned copy of the whole input), GB/s."""
+            c0 = torch.cuda.Event(enable_timing=True)
+            c1 = torch.cuda.Event(enable_timing=True)
+            c0.record(stream)
+            A.copy_(A_host, non_blocking=True)
+            c1.record(stream)
+            torch.cuda.synchronize()
+            return A_host.numel() * 16 / (c0.elapsed_time(c1) * 1e6)
+
+        h2d_start = h2d_rate()
 
         def host_call():
             st = api.tokura_zgeev_batched_host(h, N, BATCH, A_host.data_ptr(), eig_host.data_ptr(),
@@ -802,12 +816,17 @@ def run_ours(args):
         e1.record(stream)
         torch.cuda.synchronize()
         single_ms = max_over_ranks(e0.elapsed_time(e1) / max(1, args.steps // 2), dist, dev)
+        # The host link's rate on this machine before and after the steps: it sets how much of the
+        # copy the chunked host-buffer call can hide.
+        h2d_gbs = {"start": h2d_start, "end": h2d_rate()}
         e2e = {"value": ws * BATCH / (e_ms * 1e-3), "unit": "matrices/s",
                "h2d_bytes_per_step": A_host.numel() * 16,
                "d2h_bytes_per_step": eig_host.numel() * 16 + flag_host.numel(),
-               "ms_per_step": e_ms, "api": "tokura_zgeev_batched_host (pinned host buffers, wall clock)",
+               "ms_per_step": e_ms,
+               "api": "tokura_zgeev_batched_host (pinned huge-page host buffers from tokuraHostAlloc, wall clock)",
                "flagged": host_flagged,
-               "single_stream": {"value": ws * BATCH / (single_ms * 1e-3), "ms_per_step": single_ms}}
+               "single_stream": {"value": ws * BATCH / (single_ms * 1e-3), "ms_per_step": single_ms},
+               "h2d_gbs": h2d_gbs}
         del A_host, eig_host, flag_host
     del A, eig, flag, work
     torch.cuda.empty_cache()

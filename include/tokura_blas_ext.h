@@ -161,10 +161,28 @@ TOKURA_API size_t tokura_get_zgeev_vectors_workspacesize(int n, int batch_count)
 /* Lanes per matrix of the ragged solvers (1, 2, 4, 8; 0 = chosen per launch). */
 TOKURA_API int tokuraSetRaggedLanes(tokurablas_t* handle, int lanes_per_matrix);
 
+/* Pinned host memory for host-buffer calls: anonymous memory aligned to and
+ * backed by transparent huge pages where the kernel allows, registered with
+ * CUDA (cudaHostRegister). Copies from it keep the host link's full rate after
+ * idle periods, where copies from cudaHostAlloc memory (base pages, one IOMMU
+ * translation each) slow down. Free with tokuraHostFree.
+ * Returns 0; -1 ptr NULL, -2 bytes == 0; 2 mapping failed, 1 registration failed. */
+TOKURA_API int tokuraHostAlloc(void** ptr, size_t bytes);
+/* Frees memory from tokuraHostAlloc (NULL: no-op). Returns 0; -1 not from
+ * tokuraHostAlloc (or already freed); 1 CUDA unregistration failed. */
+TOKURA_API int tokuraHostFree(void* ptr);
+
+/* Host-to-device rate (GB/s) that tokura_zgeev_batched_host plans its chunks
+ * for; 0 (the default) uses the rate its previous call on the handle measured.
+ * Returns 0; -1 NULL handle, -2 gbs negative or not finite. */
+TOKURA_API int tokuraSetHostLinkRate(tokurablas_t* handle, double gbs);
+
 /* Host-buffer variant of tokura_zgeev_batched_gpu: A, eigenvalues and flag are
  * HOST pointers (layouts as the device call). The batch is cut into chunks of
- * chunk_matrices (0 = automatic) issued round-robin on the handle's own
- * streams, so host-device copies overlap the solves; returns when the results
+ * chunk_matrices (0 = automatic: 4 equal chunks, or growing chunks from 1/16
+ * of the batch when the previous call on the handle saw a host-to-device rate
+ * below 100 GB/s) issued round-robin on the handle's own streams, copies in
+ * chunk order, so host-device copies overlap the solves; returns when the results
  * are in host memory. Replaces the reference's multi-stream example driver
  * (stream_test_with_MKL/main.cu:236-288). Host memory should be pinned for the
  * copies to overlap. Device buffers are cached in the handle (freed by

@@ -133,6 +133,15 @@ def test_create_destroy_null(lib):
     assert lib.tokuraSetSweepCap(None, 3) == -1
     assert lib.tokuraSetBalancing(None, 3) == -1
     assert lib.tokuraSetShiftHints(None, 1) == -1
+    assert lib.tokuraSetHostLinkRate(None, 10.0) == -1
+    # Host allocator: argument checks and unknown pointers need no GPU.
+    p = ctypes.c_void_p()
+    assert lib.tokuraHostAlloc(None, 16) == -1
+    assert lib.tokuraHostAlloc(ctypes.byref(p), 0) == -2 and p.value is None
+    assert lib.tokuraHostFree(None) == 0
+    buf = ctypes.create_string_buffer(64)
+    assert lib.tokuraHostFree(ctypes.cast(buf, ctypes.c_void_p)) == -1
+    assert lib.tokuraSetRaggedLanes(None, 2) == -1
 
 
 def test_reference_style_caller_links(tmp_path, lib):

@@ -42,19 +42,59 @@ def test_host_entry_argument_codes(cuda):
     assert f(h, 2, 1, p, p, p, -1) == -8
 
 
+@pytest.mark.parametrize("link_gbs", [0.0, 10.0, 1000.0])
 @pytest.mark.parametrize("batch", [3000, 10000, 40000])
-def test_host_entry_growing_chunks_bitwise_equal_device_call(cuda, batch):
-    """The default chunk plan (1/16, 1/16, 1/8, 1/4, 1/2 of the batch, each at
-    least 1,024 matrices) cuts the batch differently from the device call, but
-    every matrix is solved by the same arithmetic: bitwise the same results."""
+def test_host_entry_default_plans_bitwise_equal_device_call(cuda, batch, link_gbs):
+    """Both default chunk plans (slow link: 1/16, 1/16, 1/8, 1/4, 1/2 of the
+    batch; fast link: 4 equal chunks; each at least 1,024 matrices) cut the
+    batch differently from the device call, but every matrix is solved by the
+    same arithmetic: bitwise the same results. 0 = the measured rate: the
+    second call plans with the rate the first one saw."""
     import torch
 
     n = 16
     A = wl.torch_gaussian(batch, n, seed=batch)
     w_dev, f_dev = api.zgeev_batched(A)
     torch.cuda.synchronize()
+    h = api.Handle()
+    assert h.set_host_link_rate(link_gbs) == 0
     # zgeev_batched reads the row-major tensor as column-major A^T; pass the same buffer.
     A_host = A.cpu().pin_memory()
-    w_host, f_host = api.zgeev_batched_host(A_host)
-    assert np.array_equal(w_host.view(np.uint64), w_dev.cpu().numpy().view(np.uint64))
-    assert np.array_equal(f_host, f_dev.cpu().numpy())
+    for _ in range(2):
+        w_host, f_host = api.zgeev_batched_host(A_host, handle=h)
+        assert np.array_equal(w_host.view(np.uint64), w_dev.cpu().numpy().view(np.uint64))
+        assert np.array_equal(f_host, f_dev.cpu().numpy())
+
+
+def test_set_host_link_rate_validation(cuda):
+    h = api.Handle()
+    assert h.set_host_link_rate(0.0) == 0 and h.set_host_link_rate(25.5) == 0
+    assert h.set_host_link_rate(-1.0) == -2 and h.set_host_link_rate(float("nan")) == -2
+    assert h.set_host_link_rate(float("inf")) == -2
+
+
+def test_host_alloc_buffers_feed_the_host_entry(cuda):
+    """tokuraHostAlloc memory (pinned, huge pages past one huge page) through the
+    host entry point: bitwise the device call's results; explicit alloc/free codes."""
+    import ctypes
+    import gc
+
+    import torch
+
+    n, batch = 32, 80000  # 1.3 GB of input: spans more than one huge page
+    A = wl.torch_gaussian(batch, n, seed=5)
+    A_h = api.host_empty(A.shape, A.dtype)
+    assert A_h.is_pinned() and A_h.shape == A.shape and A_h.dtype == A.dtype
+    A_h.copy_(A)
+    w_dev, f_dev = api.zgeev_batched(A)
+    torch.cuda.synchronize()
+    w_h, f_h = api.zgeev_batched_host(A_h)
+    assert np.array_equal(w_h.view(np.uint64), w_dev.cpu().numpy().view(np.uint64))
+    assert np.array_equal(f_h, f_dev.cpu().numpy())
+    del A_h
+    gc.collect()
+    p = ctypes.c_void_p()
+    assert api.lib().tokuraHostAlloc(ctypes.byref(p), 1000) == 0 and p.value
+    ctypes.memset(p, 7, 1000)
+    assert api.lib().tokuraHostFree(p) == 0
+    assert api.lib().tokuraHostFree(p) == -1

@@ -11,6 +11,7 @@ from .api import (  # noqa: F401
     dgeev_batched,
     default_handle,
     exported_symbols,
+    host_empty,
     lib,
     tokura_get_zgeeveigenvaluesgetworspacesize,
     tokura_zgeev_batched_gpu,

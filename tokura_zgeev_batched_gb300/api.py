@@ -52,6 +52,9 @@ _SIGNATURES = {
     ),
     "tokura_get_zgeev_ragged_workspacesize": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_longlong]),
     "tokuraSetRaggedLanes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "tokuraSetHostLinkRate": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
+    "tokuraHostAlloc": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_size_t]),
+    "tokuraHostFree": (ctypes.c_int, [ctypes.c_void_p]),
     "tokuraAutotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
     "tokuraAutotuneRagged": (ctypes.c_int,
                              [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
@@ -173,6 +176,10 @@ class Handle:
 
     def set_ragged_lanes(self, lanes: int) -> int:
         return int(lib().tokuraSetRaggedLanes(self.ptr, int(lanes)))
+
+    def set_host_link_rate(self, gbs: float) -> int:
+        """Host-to-device GB/s the host-buffer call plans for (0 = the rate its last call measured)."""
+        return int(lib().tokuraSetHostLinkRate(self.ptr, float(gbs)))
 
     def close(self):
         if self.ptr is not None and self.ptr.value:
@@ -587,10 +594,46 @@ def tokura_zgeev_batched_host(handle, n: int, batch_count: int, A: int, eigenval
                                                int(chunk_matrices)))
 
 
+class HostBlock:
+    """Owns memory from tokuraHostAlloc (pinned, on huge pages); freed when the last reference goes."""
+
+    def __init__(self, nbytes: int):
+        p = ctypes.c_void_p()
+        st = lib().tokuraHostAlloc(ctypes.byref(p), int(nbytes))
+        if st != 0:
+            raise RuntimeError(f"tokuraHostAlloc returned {st}")
+        self.ptr = p.value
+        self.nbytes = int(nbytes)
+
+    def __del__(self):
+        if getattr(self, "ptr", None):
+            lib().tokuraHostFree(ctypes.c_void_p(self.ptr))
+            self.ptr = None
+
+
+def host_empty(shape, dtype):
+    """Uninitialised CPU torch tensor in tokuraHostAlloc memory (pinned, huge pages): the host
+    buffers for :func:`zgeev_batched_host` / ``tokura_zgeev_batched_host``."""
+    import math
+
+    import numpy as np
+    import torch
+
+    shape = tuple(int(s) for s in shape)
+    itemsize = torch.empty((), dtype=dtype).element_size()
+    nbytes = max(1, math.prod(shape)) * itemsize
+    block = HostBlock(nbytes)
+    raw = (ctypes.c_uint8 * nbytes).from_address(block.ptr)
+    raw.block = block  # tensor -> numpy array -> raw -> block: freed with the last view
+    t = torch.from_numpy(np.ctypeslib.as_array(raw)).view(dtype)
+    return t[: math.prod(shape)].view(shape)
+
+
 def zgeev_batched_host(A, handle: Handle | None = None, chunk_matrices: int = 0):
     """Eigenvalues of host-resident matrices (numpy complex128 ``[..., n, n]`` or a CPU torch tensor).
 
-    Pinned (page-locked) torch tensors let the copies overlap the solves.
+    Pinned (page-locked) torch tensors let the copies overlap the solves; :func:`host_empty`
+    gives pinned memory on huge pages, which keeps the host link at full rate.
     Returns numpy ``(eigenvalues[..., n], flag[...])``.
     """
     import numpy as np

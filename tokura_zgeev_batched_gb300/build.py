@@ -41,6 +41,7 @@ SOURCES = [
     "tokura_capi.cpp",
     "compat_cxx.cpp",
     "tokura_host_pipeline.cpp",
+    "tokura_host_alloc.cpp",
 ]
 
 

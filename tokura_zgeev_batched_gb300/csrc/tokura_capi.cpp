@@ -149,6 +149,14 @@ extern "C" int tokura_zgeev_ragged_gpu(tokurablas_t* handle, int batch_count, co
   return err == cudaSuccess ? 0 : 1;
 }
 
+extern "C" int tokuraSetHostLinkRate(tokurablas_t* handle, double gbs) {
+  if (handle == nullptr) return -1;
+  if (!(gbs >= 0.0 && gbs < 1e9)) return -2;  // also rejects NaN
+  std::lock_guard<std::mutex> lock(handle->pipe_mutex);
+  handle->pipe.link_gbs_fixed = gbs;
+  return 0;
+}
+
 extern "C" int tokuraSetRaggedLanes(tokurablas_t* handle, int lanes_per_matrix) {
   if (handle == nullptr) return -1;
   if (!(lanes_per_matrix == 0 || lanes_per_matrix == 1 || lanes_per_matrix == 2 || lanes_per_matrix == 4 ||

@@ -15,6 +15,10 @@ struct HostPipeline {
   void* d_work[kStreams] = {};
   char* d_flag[kStreams] = {};
   cudaStream_t stream[kStreams] = {};
+  cudaEvent_t copied[kStreams] = {};  // end of the host-to-device copy last issued on each stream
+  cudaEvent_t copy_begin = nullptr, copy_end = nullptr;  // timing of one call's host-to-device copies
+  double link_gbs = 0.0;  // host-to-device rate seen by the last call (GB/s; 0 = not measured yet)
+  double link_gbs_fixed = 0.0;  // rate set by tokuraSetHostLinkRate (> 0 replaces the measured one)
   size_t cap_a[kStreams] = {}, cap_eig[kStreams] = {}, cap_work[kStreams] = {}, cap_flag[kStreams] = {};
   void release();
 };
