@@ -139,6 +139,7 @@ def test_create_destroy_null(lib):
     assert lib.tokuraHostAlloc(None, 16) == -1
     assert lib.tokuraHostAlloc(ctypes.byref(p), 0) == -2 and p.value is None
     assert lib.tokuraHostFree(None) == 0
+    assert lib.tokuraHostAlloc(ctypes.byref(p), 2 ** 64 - 1) == 2 and p.value is None
     buf = ctypes.create_string_buffer(64)
     assert lib.tokuraHostFree(ctypes.cast(buf, ctypes.c_void_p)) == -1
     assert lib.tokuraSetRaggedLanes(None, 2) == -1

@@ -607,7 +607,10 @@ class HostBlock:
 
     def __del__(self):
         if getattr(self, "ptr", None):
-            lib().tokuraHostFree(ctypes.c_void_p(self.ptr))
+            try:
+                lib().tokuraHostFree(ctypes.c_void_p(self.ptr))
+            except Exception:  # noqa: BLE001 - interpreter shutdown: the process unmaps it anyway
+                pass
             self.ptr = None
 
 

@@ -51,6 +51,7 @@ extern "C" TOKURA_API int tokuraHostAlloc(void** ptr, size_t bytes) {
   if (bytes == 0) return -2;
   const size_t page = (size_t)sysconf(_SC_PAGESIZE);
   const size_t hp = huge_page_bytes();
+  if (bytes > ~(size_t)0 - 2 * (hp > page ? hp : page)) return 2;  // the rounded mapping would overflow
   const size_t len = round_up(bytes, page);
   const bool huge = hp > page && len >= hp;
   // Map with room to align the start to a huge page, then trim both ends.
