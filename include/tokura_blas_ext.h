@@ -37,14 +37,22 @@ TOKURA_API int tokuraSetBalancing(tokurablas_t* handle, int mode);
  * estimate as the shift of the first sweep after each deflation (about 2.1
  * sweeps per eigenvalue instead of 3.4). Modes: 1 (default) for the plain,
  * strided, pointer-array, complex64, host-buffer and workspace-free entry
- * points with n >= 12; 2 for every eigenvalue entry point and order,
- * including the ragged one (where it does not pay off today); 0 off
+ * points with n >= 12, and the ragged entry point for its matrices of order
+ * >= tokuraSetRaggedHintMinOrder's value; 2 for every eigenvalue entry
+ * point and order, ragged included; 0 off
  * (Wilkinson shifts only). Results keep the FP64 accuracy in every mode (the
  * estimates only steer the iteration; results are not bitwise identical
  * between modes). The estimates use 8n bytes per matrix of the workspace
  * after the staging area, inside the reference's workspace formula.
  * Returns 0, -1 NULL handle, -2 bad mode. */
 TOKURA_API int tokuraSetShiftHints(tokurablas_t* handle, int mode);
+
+/* Smallest order whose matrices get shift hints in ragged calls under mode 1
+ * (1..64; 65 = none; default 48). The estimator costs about n^2 per matrix
+ * and saves about n^3 of QR work, so on mixed orders it pays on the largest
+ * (200,000 orders in U{1..64}: 676 ms without hints, 645 ms with 48).
+ * Returns 0, -1 NULL handle, -2 n outside 1..65. */
+TOKURA_API int tokuraSetRaggedHintMinOrder(tokurablas_t* handle, int n);
 
 /* Launch shape of the plain kernel for order n: lanes per matrix (1, 2, 4, 8;
  * 0 = choose from the batch size) and threads per block (32..256, multiple

@@ -134,6 +134,7 @@ def test_create_destroy_null(lib):
     assert lib.tokuraSetBalancing(None, 3) == -1
     assert lib.tokuraSetShiftHints(None, 1) == -1
     assert lib.tokuraSetHostLinkRate(None, 10.0) == -1
+    assert lib.tokuraSetRaggedHintMinOrder(None, 48) == -1
     # Host allocator: argument checks and unknown pointers need no GPU.
     p = ctypes.c_void_p()
     assert lib.tokuraHostAlloc(None, 16) == -1

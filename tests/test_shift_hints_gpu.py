@@ -131,9 +131,10 @@ def test_hints_on_every_layout_match_contiguous(cuda):
 
 
 @pytest.mark.parametrize("lanes", [0, 1, 4])
-def test_ragged_with_hints_everywhere(cuda, lanes):
-    """Mode 2 runs the ragged forward in two phases with the estimator beside
-    the first; parity with LAPACK and identical flags to mode 0."""
+def test_ragged_with_hints(cuda, lanes):
+    """Modes 1 (orders >= 20 here) and 2 (every order) run the ragged forward
+    in two phases with the estimator beside the first; parity with LAPACK and
+    identical flags to mode 0."""
     import torch
     from tokura_zgeev_batched_gb300 import api
 
@@ -144,22 +145,32 @@ def test_ragged_with_hints_everywhere(cuda, lanes):
     mats[40][0, 0] = np.inf
     buf, ns, offs, eoffs = wl.pack_ragged([np.ascontiguousarray(m.T) for m in mats])
     out = {}
-    for mode in (0, 2):
+    for mode in (0, 1, 2):
         h = api.Handle()
         assert h.set_shift_hints(mode) == 0 and h.set_ragged_lanes(lanes) == 0
+        assert h.set_ragged_hint_min_order(20) == 0
         eig, flag = api.zgeev_ragged(torch.from_numpy(buf).cuda(), torch.from_numpy(ns).cuda(), handle=h)
         torch.cuda.synchronize()
         out[mode] = (eig.cpu().numpy(), flag.cpu().numpy())
-    assert np.array_equal(out[0][1], out[2][1])
-    eig, flag = out[2]
-    assert flag[40] == 2 and flag[17] == 0 and (np.delete(flag, 40) == 0).all()
-    for k, m in enumerate(mats):
-        if k == 40:
-            continue
-        n = m.shape[0]
-        got = eig[eoffs[k]: eoffs[k] + n]
-        if k == 17:
-            assert (got == 0).all()
-            continue
-        w_ref = lo.zgeev(np.ascontiguousarray(m.T)[None])[0][0]
-        assert lo.matched_abs_errors(got, w_ref).max() <= lo.TOL_REL_FRO * np.linalg.norm(m), k
+    for mode in (1, 2):
+        assert np.array_equal(out[0][1], out[mode][1])
+        eig, flag = out[mode]
+        assert flag[40] == 2 and flag[17] == 0 and (np.delete(flag, 40) == 0).all()
+        for k, m in enumerate(mats):
+            if k == 40:
+                continue
+            n = m.shape[0]
+            got = eig[eoffs[k]: eoffs[k] + n]
+            if k == 17:
+                assert (got == 0).all()
+                continue
+            w_ref = lo.zgeev(np.ascontiguousarray(m.T)[None])[0][0]
+            assert lo.matched_abs_errors(got, w_ref).max() <= lo.TOL_REL_FRO * np.linalg.norm(m), (mode, k)
+
+
+def test_set_ragged_hint_min_order_validation(cuda):
+    from tokura_zgeev_batched_gb300 import api
+
+    h = api.Handle()
+    assert h.set_ragged_hint_min_order(1) == 0 and h.set_ragged_hint_min_order(65) == 0
+    assert h.set_ragged_hint_min_order(0) == -2 and h.set_ragged_hint_min_order(66) == -2

@@ -53,6 +53,7 @@ _SIGNATURES = {
     "tokura_get_zgeev_ragged_workspacesize": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_longlong]),
     "tokuraSetRaggedLanes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "tokuraSetHostLinkRate": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_double]),
+    "tokuraSetRaggedHintMinOrder": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "tokuraHostAlloc": (ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_size_t]),
     "tokuraHostFree": (ctypes.c_int, [ctypes.c_void_p]),
     "tokuraAutotune": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_void_p]),
@@ -176,6 +177,10 @@ class Handle:
 
     def set_ragged_lanes(self, lanes: int) -> int:
         return int(lib().tokuraSetRaggedLanes(self.ptr, int(lanes)))
+
+    def set_ragged_hint_min_order(self, n: int) -> int:
+        """Ragged calls under shift-hint mode 1 estimate orders >= n (65: none)."""
+        return int(lib().tokuraSetRaggedHintMinOrder(self.ptr, int(n)))
 
     def set_host_link_rate(self, gbs: float) -> int:
         """Host-to-device GB/s the host-buffer call plans for (0 = the rate its last call measured)."""

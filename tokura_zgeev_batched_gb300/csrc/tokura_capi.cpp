@@ -145,7 +145,7 @@ extern "C" int tokura_zgeev_ragged_gpu(tokurablas_t* handle, int batch_count, co
                                              total_elements, reinterpret_cast<const double2*>(A),
                                              reinterpret_cast<double2*>(eigenvalues), work, flag,
                                              handle->itmax_override, stream, handle->balance_mode,
-                                             tzg::use_ragged_shift_hints(handle), &handle->fj);
+                                             tzg::ragged_hint_min_order(handle), &handle->fj);
   return err == cudaSuccess ? 0 : 1;
 }
 
@@ -154,6 +154,13 @@ extern "C" int tokuraSetHostLinkRate(tokurablas_t* handle, double gbs) {
   if (!(gbs >= 0.0 && gbs < 1e9)) return -2;  // also rejects NaN
   std::lock_guard<std::mutex> lock(handle->pipe_mutex);
   handle->pipe.link_gbs_fixed = gbs;
+  return 0;
+}
+
+extern "C" int tokuraSetRaggedHintMinOrder(tokurablas_t* handle, int n) {
+  if (handle == nullptr) return -1;
+  if (!(n >= 1 && n <= TOKURA_ZGEEV_BATCHED_MAX_MATRIX_SIZE + 1)) return -2;
+  handle->ragged_hint_min_n = n;
   return 0;
 }
 

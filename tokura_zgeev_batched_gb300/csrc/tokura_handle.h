@@ -34,6 +34,7 @@ struct tokurablas_t {
   tzg::PlainConfig real[65] = {};  // the same for the real (dgeev/sgeev) kernel
   int ragged_lanes = 0;  // lanes per matrix of the ragged solvers; 0 = chosen per launch
   int balance_mode = 0;  // balancing before the eigenvalue solves: 0 none (the reference's behaviour) .. 3 both
+  int ragged_hint_min_n = 48;  // mode 1: ragged matrices of this order and above get hints (65: none)
   int shift_hints = 1;   // FP32 eigenvalue estimates as first shifts: 0 off, 1 uniform batches with
                          // n >= kShiftHintMinN, 2 every eigenvalue entry point and order (ragged too)
   tzg::HostPipeline pipe;  // host-buffer entry point state (guarded by pipe_mutex)
@@ -95,11 +96,18 @@ inline bool use_shift_hints(const tokurablas_t* h, int n) {
   return h->shift_hints == 2 || (h->shift_hints == 1 && n >= kShiftHintMinN);
 }
 
-// The ragged solver takes hints only when asked for everywhere: its
-// estimator (one pass over the whole batch, 225 ms for 200,000 orders in
-// U{1..64}) outlasts the Hessenberg phase it runs beside (157 ms), so with
-// hints the solve measured 690 ms against 670 ms without.
-inline bool use_ragged_shift_hints(const tokurablas_t* h) { return h->shift_hints == 2; }
+// Smallest order the ragged solver computes hints for (0: none). Mode 2:
+// every order. Mode 1: orders >= ragged_hint_min_n (65: none). The
+// estimator's cost grows like n^2 per matrix (rotation rounds) and the QR work
+// it saves like n^3, so for mixed orders it pays on the large ones. On
+// 200,000 orders in U{1..64}: no hints 676 ms; hints for every order 662 ms
+// (the estimator, 225 ms, outlasts the Hessenberg phase it runs beside,
+// 157 ms); orders >= 56: 650, >= 48: 645, >= 40: 652, >= 32: 657 ms.
+inline int ragged_hint_min_order(const tokurablas_t* h) {
+  if (h->shift_hints == 2) return 1;
+  if (h->shift_hints == 1 && h->ragged_hint_min_n <= 64) return h->ragged_hint_min_n;
+  return 0;
+}
 
 
 }  // namespace tzg

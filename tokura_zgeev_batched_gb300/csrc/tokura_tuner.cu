@@ -152,7 +152,7 @@ extern "C" TOKURA_API int tokuraAutotuneRagged(tokurablas_t* handle, int batch_c
     const float ms = time_launches(stream, 2, [&]() {
       return launch_ragged(lanes, handle->sm_count, batch_count, n, off, nullptr, total, A,
                            static_cast<double2*>(b.p[1]), b.p[2], static_cast<char*>(b.p[3]), 0, stream, 0,
-                           use_ragged_shift_hints(handle), &handle->fj);
+                           ragged_hint_min_order(handle), &handle->fj);
     }, &err);
     if (err != cudaSuccess) return 1;
     if (ms < best) {

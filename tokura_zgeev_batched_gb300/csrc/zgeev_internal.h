@@ -43,7 +43,7 @@ size_t ragged_workspace_bytes(int batch, long long total_elements);
 cudaError_t launch_ragged(int lanes, int sms, int batch, const int* n, const long long* offsets,
                           const long long* eig_offsets, long long total_elements, const double2* A, double2* eig,
                           void* work, char* flag, int itmax_override, cudaStream_t stream, int balance = 0,
-                          bool hints = false, const ForkJoin* fj = nullptr);
+                          int hint_min_n = 0, const ForkJoin* fj = nullptr);
 
 // Backward (Abar from A, eigenvalues and their gradients).
 size_t backward_workspace_bytes(int n, int batch);

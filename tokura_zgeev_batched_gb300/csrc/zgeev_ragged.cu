@@ -170,8 +170,10 @@ static cudaError_t ragged_prepare(int lanes, int sms, int batch, const int* n, c
 
 cudaError_t launch_ragged(int lanes, int sms, int batch, const int* n, const long long* offsets,
                           const long long* eig_offsets, long long total_elements, const double2* A, double2* eig,
-                          void* work, char* flag, int itmax_override, cudaStream_t stream, int balance, bool hints,
-                          const ForkJoin* fj) {
+                          void* work, char* flag, int itmax_override, cudaStream_t stream, int balance,
+                          int hint_min_n, const ForkJoin* fj) {
+  // Shift hints for the matrices of order >= hint_min_n (0: none).
+  const bool hints = hint_min_n > 0 && hint_min_n <= kMaxN;
   if (lanes == 0) lanes = ragged_auto_lanes(sms, batch, total_elements);
   if (!(lanes == 1 || lanes == 2 || lanes == 4 || lanes == 8)) return cudaErrorInvalidValue;
   const RaggedLayout lay = ragged_layout(batch, total_elements);
@@ -184,9 +186,9 @@ cudaError_t launch_ragged(int lanes, int sms, int batch, const int* n, const lon
   cudaError_t err = cudaSuccess;
   if (split) {  // the estimator starts first, beside the planning and the prepare phase
     lock = std::unique_lock<std::mutex>(*fj->mu);
-    err = ragged_fork_estimates(sms, batch, n, offsets, total_elements, A, est, stream, *fj);
+    err = ragged_fork_estimates(sms, batch, n, offsets, total_elements, A, est, hint_min_n, stream, *fj);
   } else if (hints) {
-    err = launch_ragged_estimates(sms, batch, n, offsets, total_elements, A, est, stream);
+    err = launch_ragged_estimates(sms, batch, n, offsets, total_elements, A, est, hint_min_n, stream);
   }
   if (err != cudaSuccess) return err;
   RaggedPlan* plan;
@@ -196,7 +198,7 @@ cudaError_t launch_ragged(int lanes, int sms, int batch, const int* n, const lon
                        &sorted, &eo);
   if (err != cudaSuccess) return err;
   const RaggedArgs args{offsets, eo, A, eig, nullptr, nullptr, nullptr, stage, total_elements, flag, sorted,
-                        itmax_override, balance, est, state};
+                        itmax_override, balance, est, state, hint_min_n};
   if (split) return ragged_launch_phases(lanes, sms, plan, args, balance != 0, stream, *fj);
   if (balance != 0) return launch_ragged_kernel<false, true, kPhaseAll>(lanes, sms, plan, args, stream);
   return launch_ragged_kernel<false, false, kPhaseAll>(lanes, sms, plan, args, stream);
@@ -217,7 +219,7 @@ cudaError_t launch_ragged_backward(int lanes, int sms, int batch, const int* n, 
                                    stream, &plan, &sorted, &eo);
   if (err != cudaSuccess) return err;
   const RaggedArgs args{offsets, eo, A, nullptr, lam, gbar, gA, stage, total_elements, flag, sorted, itmax_override,
-                        0, nullptr, nullptr};
+                        0, nullptr, nullptr, 0};
   return launch_ragged_kernel<true, false, kPhaseAll>(lanes, sms, plan, args, stream);
 }
 

@@ -87,6 +87,7 @@ struct RaggedArgs {
   int balance;           // forward: balancing mode
   const float2* est;     // forward: FP32 shift hints, kMaxN per matrix (or null)
   int* state;            // forward, split solve: pre-scaling exponent or kStateDone per matrix
+  int est_min_n;         // forward: orders from which est holds hints
 };
 
 // Tile scheduling. Tiles are numbered in descending-work order; SM s owns
@@ -142,6 +143,7 @@ __global__ void __launch_bounds__(128) zgeev_ragged_kernel(RaggedPlan* plan, Rag
       const long long nn = (long long)nb * nb;
       double2* base = a.stage + bin.stage + (long long)u * TW * nn + slot;
       const int itmax = a.itmax_override > 0 ? a.itmax_override : default_itmax(nb);
+      const float2* est = a.est != nullptr && nb >= a.est_min_n ? a.est + (long long)j * kMaxN : nullptr;
       int status = kPrepared;  // kPrepared: no flag to write yet
       if (kBackward) {
         BwdViews V{MatView{base, nb, tw}, MatView{base + a.region, nb, tw}, MatView{base + 2 * a.region, nb, tw},
@@ -150,7 +152,7 @@ __global__ void __launch_bounds__(128) zgeev_ragged_kernel(RaggedPlan* plan, Rag
                                     a.gA + a.offsets[j], V, G, itmax);
       } else if (kPhase == kPhaseAll) {
         status = solve_matrix<L, kBalance>(a.A + a.offsets[j], MatView{base, nb, tw}, G, a.eig + a.eoff[j], itmax,
-                                           a.balance, a.est != nullptr ? a.est + (long long)j * kMaxN : nullptr);
+                                           a.balance, est);
       } else if (kPhase == kPhasePrepare) {
         int shift;
         status = prepare_matrix<L, kBalance>(SrcContig{a.A + a.offsets[j]}, MatView{base, nb, tw}, G,
@@ -159,8 +161,7 @@ __global__ void __launch_bounds__(128) zgeev_ragged_kernel(RaggedPlan* plan, Rag
       } else {
         const int s = a.state[j];
         if (s != kStateDone)
-          status = qr_eigenvalues<L>(MatView{base, nb, tw}, G, a.eig + a.eoff[j], s, itmax,
-                                     a.est + (long long)j * kMaxN);
+          status = qr_eigenvalues<L>(MatView{base, nb, tw}, G, a.eig + a.eoff[j], s, itmax, est);
       }
       if (G.rank == 0 && status != kPrepared) a.flag[j] = (char)status;
     }
@@ -201,12 +202,13 @@ inline cudaError_t launch_ragged_kernel(int lanes, int sms, RaggedPlan* plan, co
 }
 
 // Defined in zgeev_ragged_split.cu (the hinted, two-phase forward).
-// Estimator for every valid matrix of the batch, on `stream`.
+// Estimator for every valid matrix of order >= min_n, on `stream`.
 cudaError_t launch_ragged_estimates(int sms, int batch, const int* n, const long long* offsets, long long total,
-                                    const double2* A, float2* est, cudaStream_t stream);
+                                    const double2* A, float2* est, int min_n, cudaStream_t stream);
 // Fork from `stream` to fj.aux, estimator there (call with *fj.mu held).
 cudaError_t ragged_fork_estimates(int sms, int batch, const int* n, const long long* offsets, long long total,
-                                  const double2* A, float2* est, cudaStream_t stream, const ForkJoin& fj);
+                                  const double2* A, float2* est, int min_n, cudaStream_t stream,
+                                  const ForkJoin& fj);
 // Prepare phase on `stream`, join with the estimator, QR phase (*fj.mu held).
 cudaError_t ragged_launch_phases(int lanes, int sms, RaggedPlan* plan, const RaggedArgs& args, bool balance,
                                  cudaStream_t stream, const ForkJoin& fj);

@@ -9,21 +9,22 @@
 namespace tzg {
 
 // One warp per matrix in index order (shared memory sized for n = 64);
-// invalid entries are skipped (the planner flags them).
+// invalid entries (the planner flags them) and orders below min_n are skipped.
 __global__ void __launch_bounds__(32) ragged_estimate_kernel(int batch, const int* __restrict__ n,
                                                              const long long* __restrict__ offsets, long long total,
-                                                             const double2* __restrict__ A, float2* __restrict__ est) {
+                                                             const double2* __restrict__ A, float2* __restrict__ est,
+                                                             int min_n) {
   extern __shared__ float2 ragged_estimate_smem[];
   for (long long j = blockIdx.x; j < batch; j += gridDim.x) {
     const int nj = n[j];
     const long long off = offsets[j];
-    if (!ragged_valid(nj, off, total)) continue;
+    if (nj < min_n || !ragged_valid(nj, off, total)) continue;
     estimate_matrix(SrcContig{A + off}, nj, ragged_estimate_smem, est + j * kMaxN);
   }
 }
 
 cudaError_t launch_ragged_estimates(int sms, int batch, const int* n, const long long* offsets, long long total,
-                                    const double2* A, float2* est, cudaStream_t stream) {
+                                    const double2* A, float2* est, int min_n, cudaStream_t stream) {
   const size_t smem = sizeof(float2) * kMaxN * (kMaxN + 1);
   int per_sm = 0;
   const cudaError_t err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, ragged_estimate_kernel, 32, smem);
@@ -31,16 +32,18 @@ cudaError_t launch_ragged_estimates(int sms, int batch, const int* n, const long
   if (per_sm < 1) per_sm = 1;
   long long blocks = (long long)(sms > 0 ? sms : 1) * per_sm;
   if (blocks > batch) blocks = batch;
-  ragged_estimate_kernel<<<(unsigned)blocks, 32, smem, stream>>>(batch, n, offsets, total, A, est);
+  ragged_estimate_kernel<<<(unsigned)blocks, 32, smem, stream>>>(batch, n, offsets, total, A, est, min_n);
   return cudaGetLastError();
 }
 
 cudaError_t ragged_fork_estimates(int sms, int batch, const int* n, const long long* offsets, long long total,
-                                  const double2* A, float2* est, cudaStream_t stream, const ForkJoin& fj) {
+                                  const double2* A, float2* est, int min_n, cudaStream_t stream,
+                                  const ForkJoin& fj) {
   cudaError_t err;
   if ((err = cudaEventRecord(fj.fork, stream)) != cudaSuccess) return err;
   if ((err = cudaStreamWaitEvent(fj.aux, fj.fork, 0)) != cudaSuccess) return err;
-  if ((err = launch_ragged_estimates(sms, batch, n, offsets, total, A, est, fj.aux)) != cudaSuccess) return err;
+  if ((err = launch_ragged_estimates(sms, batch, n, offsets, total, A, est, min_n, fj.aux)) != cudaSuccess)
+    return err;
   return cudaEventRecord(fj.join, fj.aux);
 }
 
