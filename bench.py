@@ -803,13 +803,16 @@ def run_ours(args):
         host_flagged = int((flag_host != 0).sum().item())
 
         def e2e_step():
+            # One caller-side step on one stream, waiting for its results like the host-buffer call
+            # does (five steps queued back to back without a wait made later copies from this
+            # memory slow, 5-7 GB/s instead of 211, on the boxes measured; cause unknown).
             A.copy_(A_host, non_blocking=True)
             call(N, BATCH, A, eig, flag, work)
             eig_host.copy_(eig, non_blocking=True)
             flag_host.copy_(flag, non_blocking=True)
+            torch.cuda.synchronize()
 
         e2e_step()
-        torch.cuda.synchronize()
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
