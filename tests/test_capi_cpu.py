@@ -202,3 +202,15 @@ def test_ragged_argument_validation(lib):
     assert f(fake, 4, p, p, None, 100, p, p, p, None) == -7
     assert f(fake, 4, p, None, None, 100, p, p, p, p) == -8
     assert f(fake, 4, p, p, None, 0, p, p, p, p) == -9
+
+
+def test_host_alloc_without_a_gpu_fails_cleanly(lib):
+    """Without a CUDA driver the registration fails: status 1, no pointer, nothing leaked."""
+    import torch
+
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present: tokuraHostAlloc succeeds there (tests/test_host_api_gpu.py)")
+    p = ctypes.c_void_p()
+    assert lib.tokuraHostAlloc(ctypes.byref(p), 1 << 20) == 1 and p.value is None
+    with pytest.raises(RuntimeError):
+        api.host_empty((4, 4), torch.complex128)
