@@ -154,6 +154,18 @@ def read_profile_traffic() -> dict | None:
         return None
 
 
+def guarded(fn):
+    """Runs one optional configuration: a failure is reported in its place (and its traceback on
+    stderr) instead of ending the run before the JSON line."""
+    try:
+        return fn()
+    except Exception as exc:  # noqa: BLE001
+        import traceback
+
+        traceback.print_exc(file=sys.stderr)
+        return {"error": f"{type(exc).__name__}: {exc}"[:500]}
+
+
 def cpu_baseline(n: int, seconds: float = 8.0) -> dict:
     """LAPACK zgeev per matrix over all host cores on a bounded sample of the workload."""
     import numpy as np
@@ -727,7 +739,7 @@ def run_ours(args):
     ragged = None
     if not args.no_ragged:
         # The main buffers stay allocated; the ragged batch needs ~9 GB more.
-        ragged = measure_ragged(h, dev, stream, peak)
+        ragged = guarded(lambda: measure_ragged(h, dev, stream, peak))
         phase("ragged done")
 
     # Parity spot check of the timed output against LAPACK (rank 0, outside timing).
@@ -766,11 +778,19 @@ def run_ours(args):
     e2e = None
     if not args.no_e2e:
         # Pinned host buffers from the library's allocator (tokuraHostAlloc: huge pages, so the
-        # host link keeps its full rate after the idle gaps between steps).
-        A_host = api.host_empty(A.shape, A.dtype)
+        # host link keeps its full rate after the idle gaps between steps); torch's pinned memory
+        # if that allocator fails.
+        try:
+            A_host = api.host_empty(A.shape, A.dtype)
+            eig_host = api.host_empty(eig.shape, eig.dtype)
+            flag_host = api.host_empty(flag.shape, flag.dtype)
+            host_buffers = "tokuraHostAlloc (pinned, huge pages)"
+        except RuntimeError as exc:
+            A_host = torch.empty(A.shape, dtype=A.dtype, pin_memory=True)
+            eig_host = torch.empty(eig.shape, dtype=eig.dtype, pin_memory=True)
+            flag_host = torch.empty(flag.shape, dtype=flag.dtype, pin_memory=True)
+            host_buffers = f"torch pinned memory ({exc})"
         A_host.copy_(A)
-        eig_host = api.host_empty(eig.shape, eig.dtype)
-        flag_host = api.host_empty(flag.shape, flag.dtype)
         torch.cuda.synchronize()
 
         def h2d_rate():
@@ -828,7 +848,7 @@ def run_ours(args):
                "h2d_bytes_per_step": A_host.numel() * 16,
                "d2h_bytes_per_step": eig_host.numel() * 16 + flag_host.numel(),
                "ms_per_step": e_ms,
-               "api": "tokura_zgeev_batched_host (pinned huge-page host buffers from tokuraHostAlloc, wall clock)",
+               "api": "tokura_zgeev_batched_host (pinned host buffers, wall clock)", "host_buffers": host_buffers,
                "flagged": host_flagged,
                "single_stream": {"value": ws * BATCH / (single_ms * 1e-3), "ms_per_step": single_ms},
                "h2d_gbs": h2d_gbs}
@@ -838,8 +858,8 @@ def run_ours(args):
 
     phase("e2e done")
     # ---- size sweep (the other orders of the 4 GiB size-sweep configuration)
-    sweep = {}
-    if not args.no_sweep:
+    def run_sweep():
+        sweep = {}
         for cls in ("gaussian", "vdv", "companion"):
             res = {}
             for n in SWEEP_NS + (N,):
@@ -859,32 +879,36 @@ def run_ours(args):
                 del A, eig, flag, work
                 torch.cuda.empty_cache()
             sweep[cls] = res
+        return sweep
 
+    sweep = {}
     config1 = None
     if not args.no_sweep:
-        config1 = measure_config1(h, dev, stream, peak, call)
+        sweep = guarded(run_sweep)
+        torch.cuda.empty_cache()
+        config1 = guarded(lambda: measure_config1(h, dev, stream, peak, call))
     phase("sweep and config 1 done")
     config4 = config5 = None
     if not args.no_grad:
-        config4 = measure_config4(h, dev, stream, peak)
+        config4 = guarded(lambda: measure_config4(h, dev, stream, peak))
         torch.cuda.empty_cache()
         phase("config 4 done")
-        config5 = measure_config5(h, dev, stream, peak)
+        config5 = guarded(lambda: measure_config5(h, dev, stream, peak))
         phase("config 5 done")
     real = None
     if not args.no_real:
-        real = measure_real(h, dev, stream, peak)
+        real = guarded(lambda: measure_real(h, dev, stream, peak))
         torch.cuda.empty_cache()
         phase("real path done")
     vectors = None
     if not args.no_vectors:
-        vectors = measure_vectors(h, dev, stream)
+        vectors = guarded(lambda: measure_vectors(h, dev, stream))
         torch.cuda.empty_cache()
         phase("eigenvectors done")
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        cpu = cpu_baseline(N)
+        cpu = guarded(lambda: cpu_baseline(N))
 
     if rank == 0:
         out = {
