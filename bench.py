@@ -774,7 +774,8 @@ def run_ours(args):
     # tokura_zgeev_batched_host takes host pointers, pipelines chunked H2D copies,
     # solves and D2H copies over the handle's streams and returns when the
     # eigenvalues and flags are in host memory (wall-clock timed). The same
-    # steps issued back to back on one stream are reported as "single_stream".
+    # steps on one stream without chunking (copy in, solve, copy out, wait)
+    # are reported as "single_stream".
     e2e = None
     if not args.no_e2e:
         # Pinned host buffers from the library's allocator (tokuraHostAlloc: huge pages, so the
