@@ -131,34 +131,46 @@ def test_reference_algorithm_real_part_deflation_quirk():
 
 # ---- real path oracle (LAPACK dgeev via oracle/cpu_zgeev.c)
 
-def _rotation_blocks(n: int, rng) -> tuple[np.ndarray, np.ndarray]:
-    """Q^T B Q with B block diagonal: 2x2 blocks [[a, -b], [b, a]] (eigenvalues a +- ib)
-    and, for odd n, one 1x1 block. Returns (matrix, exact spectrum)."""
-    B = np.zeros((n, n))
-    lam = []
-    for k in range(0, n - 1, 2):
-        a, b = rng.uniform(-2, 2), rng.uniform(0.5, 2)
-        B[k:k + 2, k:k + 2] = [[a, -b], [b, a]]
-        lam += [a + 1j * b, a - 1j * b]
-    if n % 2:
-        B[-1, -1] = rng.uniform(-2, 2)
-        lam.append(B[-1, -1])
-    Q, _ = np.linalg.qr(rng.standard_normal((n, n)))
-    return Q.T @ B @ Q, np.array(lam)
+GOLDEN_REAL = os.path.join(os.path.dirname(__file__), "golden", "dgeev_golden.npz")
 
 
-@pytest.mark.parametrize("n", [2, 5, 16, 33])
-def test_real_oracle_known_spectra(n):
-    rng = np.random.default_rng(100 + n)
-    mats, exact = zip(*[_rotation_blocks(n, rng) for _ in range(6)])
-    A = np.stack(mats)
-    wr, wi, info, _ = lo.dgeev(A, threads=2)
-    assert (info == 0).all()
-    assert lo.check_conjugate_pairs(wr, wi)
-    # Orthogonal similarity of normal blocks: eigenvalue condition numbers are 1.
-    err = lo.matched_abs_errors(wr + 1j * wi, np.stack(exact))
-    fro = np.linalg.norm(A, axis=(1, 2))
-    assert np.all(err.max(axis=1) <= 1e-13 * fro), err.max(axis=1) / fro
+@pytest.fixture(scope="module")
+def golden_real():
+    return np.load(GOLDEN_REAL)
+
+
+def test_real_oracle_reproduces_golden(golden_real):
+    """LAPACK dgeev on this machine reproduces the stored outputs (tests/golden/make_golden_real.py)
+    within 1e-12 ||A||_F, with the same INFO and LAPACK's conjugate-pair convention."""
+    for name in cases(golden_real):
+        A = golden_real[f"{name}/A"]
+        wr, wi, info, _ = lo.dgeev(A, threads=2)
+        assert np.array_equal(info, golden_real[f"{name}/info"]), name
+        assert lo.check_conjugate_pairs(wr, wi), name
+        assert lo.check_conjugate_pairs(golden_real[f"{name}/wr"], golden_real[f"{name}/wi"]), name
+        err = lo.matched_abs_errors(wr + 1j * wi, golden_real[f"{name}/wr"] + 1j * golden_real[f"{name}/wi"])
+        scale = np.maximum(np.linalg.norm(A, axis=(1, 2)), 1e-300)
+        assert np.all(err.max(axis=1) <= 1e-12 * scale + 1e-300), name
+
+
+def test_real_oracle_known_answers(golden_real):
+    """Exact spectra (orthogonally similar rotation blocks, triangular, zero, a companion matrix
+    with known roots) within 1e-13 ||A||_F times the worst eigenvalue condition number."""
+    checked = 0
+    for name in cases(golden_real):
+        key = f"{name}/exact"
+        if key not in golden_real.files:
+            continue
+        A = golden_real[f"{name}/A"]
+        wr, wi, info, _ = lo.dgeev(A, threads=2)
+        assert (info == 0).all(), name
+        err = lo.matched_abs_errors(wr + 1j * wi, golden_real[key])
+        fro = np.linalg.norm(A, axis=(1, 2))
+        cond = 1.0 / np.maximum(golden_real[f"{name}/rconde"], 1e-300)
+        bound = np.where(fro > 0, fro, 1.0) * 1e-13 * np.maximum(cond.max(axis=1), 1.0)
+        assert np.all(err.max(axis=1) <= bound), (name, err.max(axis=1), bound)
+        checked += 1
+    assert checked >= 10
 
 
 def test_real_oracle_agrees_with_complex_oracle():
