@@ -194,3 +194,28 @@ def test_real_path_agrees_with_complex_path(cuda):
     fro = np.linalg.norm(A, axis=(1, 2))
     err = np.array([lo.matched_abs_errors(wr[k] + 1j * wi[k], w[k]).max() for k in range(128)])
     assert (err <= 1e-11 * fro).all()
+
+
+def test_golden_real_cases(cuda):
+    """GPU results against the committed real fixtures (tests/golden/make_golden_real.py):
+    LAPACK dgeev's stored outputs and the exact spectra, identical flags, LAPACK's pair convention."""
+    import os
+
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "dgeev_golden.npz"))
+    for name in [str(x) for x in g["names"]]:
+        A = g[f"{name}/A"]
+        wr, wi, f = solve(A)
+        assert np.array_equal(f != 0, g[f"{name}/info"] != 0), name
+        ok = f == 0
+        assert lo.check_conjugate_pairs(wr[ok], wi[ok]), name
+        fro = np.linalg.norm(A, axis=(1, 2))
+        fro = np.where(fro == 0, 1.0, fro)
+        cond = 1.0 / np.maximum(g[f"{name}/rconde"], 1e-300)
+        well = cond.max(axis=1) <= lo.COND_MAX
+        w = wr + 1j * wi
+        err = lo.matched_abs_errors(w, g[f"{name}/wr"] + 1j * g[f"{name}/wi"]).max(axis=1) / fro
+        assert np.all(err[well] <= TOL), (name, err)
+        key = f"{name}/exact"
+        if key in g.files:
+            e = lo.matched_abs_errors(w, g[key]).max(axis=1) / fro
+            assert np.all(e[well] <= TOL), (name, e)
