@@ -4,6 +4,11 @@
  * The reference (hirokitokura/tokura_zgeev_batched) has no counterpart for
  * these; each comment says what it adds. All data pointers are device
  * pointers; all calls are asynchronous on `stream` unless stated.
+ *
+ * Compute calls do not write the handle, so one handle serves several
+ * streams and host threads at once. The tokuraSet* calls, tokuraLoadTuning
+ * and the autotuners change its settings: make them before those calls
+ * start, not while other threads are computing with the same handle.
  */
 #ifndef TOKURA_BLAS_EXT_GB300_H
 #define TOKURA_BLAS_EXT_GB300_H

@@ -32,7 +32,11 @@ extern "C" int tokuraCreate(tokurablas_t** handle) {
       cudaEventCreateWithFlags(&h->fj.fork, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&h->fj.join, cudaEventDisableTiming) != cudaSuccess) {
     cudaGetLastError();
+    if (h->fj.aux) cudaStreamDestroy(h->fj.aux);
+    if (h->fj.fork) cudaEventDestroy(h->fj.fork);
+    if (h->fj.join) cudaEventDestroy(h->fj.join);
     h->fj.aux = nullptr;
+    h->fj.fork = h->fj.join = nullptr;
   }
   // A tuning file written by tokuraSaveTuning for this device is applied if named in the environment.
   if (const char* path = std::getenv("TOKURA_ZGEEV_TUNING_FILE")) tokuraLoadTuning(h, path);
