@@ -214,3 +214,37 @@ def test_host_alloc_without_a_gpu_fails_cleanly(lib):
     assert lib.tokuraHostAlloc(ctypes.byref(p), 1 << 20) == 1 and p.value is None
     with pytest.raises(RuntimeError):
         api.host_empty((4, 4), torch.complex128)
+
+
+def test_more_workspace_formulas(lib):
+    """Size queries of the backward, vectors and workspace-free entry points (documented in
+    include/tokura_blas_ext.h)."""
+    for n, b in ((1, 1), (16, 50000), (64, 65536)):
+        assert lib.tokura_get_zgeev_backward_workspacesize(n, b) == 48 * n * n * b + 16 * n * b
+        assert lib.tokura_get_zgeev_vectors_workspacesize(n, b) == 48 * n * n * b + 24 * n * b + 4 * b
+    for f in (lib.tokura_get_zgeev_backward_workspacesize, lib.tokura_get_zgeev_vectors_workspacesize):
+        assert f(0, 5) == 2 ** 64 - 1 and f(65, 5) == 2 ** 64 - 1 and f(8, 0) == 2 ** 64 - 2
+    rb = lib.tokura_get_zgeev_ragged_backward_workspacesize
+    assert rb(0, 100) == 2 ** 64 - 2 and rb(10, 0) == 2 ** 64 - 3
+    assert rb(1000, 1000 * 64 * 64) >= 4 * 16 * 1000 * 64 * 64  # four staging regions per element
+    assert lib.tokura_zgeev_noalloc_max_bytes() == 32 << 20
+
+
+def test_null_handle_is_rejected_first(lib):
+    """Every handle-taking entry point checks the handle before anything else (the reference's
+    order), so these need no device."""
+    p = ctypes.c_void_p(1)
+    lanes, threads = ctypes.c_int(), ctypes.c_int()
+    assert lib.tokuraAutotune(None, 1, 2, 10, None) == -1
+    assert lib.tokuraAutotuneRagged(None, 10, 1, 64, None) == -1
+    assert lib.tokuraSetPlainConfig(None, 8, 1, 32) == -1
+    assert lib.tokuraGetPlainConfig(None, 8, 10, ctypes.byref(lanes), ctypes.byref(threads)) == -1
+    assert lib.tokuraSaveTuning(None, b"/nonexistent/t") == -1 and lib.tokuraLoadTuning(None, b"/nonexistent/t") == -1
+    assert lib.tokura_zgeev_backward_gpu(None, 8, 1, p, p, p, p, p, p, None) == -1
+    assert lib.tokura_zgeev_ragged_backward_gpu(None, 1, p, p, None, 64, p, p, p, p, p, p, None) == -1
+    assert lib.tokura_zgeev_vectors_batched_gpu(None, 8, 1, p, p, p, p, p, p, None) == -1
+    assert lib.tokura_zgeev_batched_gpu_noalloc(None, 8, 1, p, p, p, None) == -1
+    assert lib.tokura_zgeev_batched_host(None, 8, 1, p, p, p, 0) == -1
+    assert lib.tokura_zgeev_strided_batched_gpu(None, 8, 1, p, 8, 64, p, 8, p, p, None) == -1
+    assert lib.tokura_zgeev_pointer_batched_gpu(None, 8, 1, p, 8, p, p, p, None) == -1
+    assert lib.tokura_probe_fp64_peak(None, None, 0, None) == -1
