@@ -33,6 +33,7 @@ BUILD_DIR = os.path.join(HERE, "_build")
 LIB_PATH = os.path.join(BUILD_DIR, "libcpu_zgeev.so")
 SRC = os.path.join(HERE, "cpu_zgeev.c")
 REF_SRC = os.path.join(HERE, "ref_algorithm.c")
+MODEL_SRC = os.path.join(HERE, "model_qr.c")
 
 TOL_REL_FRO = 1e-11
 COND_MAX = 1e3
@@ -53,14 +54,14 @@ def find_lapack() -> str:
 
 def build(force: bool = False) -> str:
     """Compiles the C harness with gcc (plain C, no vendored sources)."""
-    newest = max(os.path.getmtime(SRC), os.path.getmtime(REF_SRC))
+    newest = max(os.path.getmtime(SRC), os.path.getmtime(REF_SRC), os.path.getmtime(MODEL_SRC))
     if not force and os.path.exists(LIB_PATH) and os.path.getmtime(LIB_PATH) >= newest:
         return LIB_PATH
     os.makedirs(BUILD_DIR, exist_ok=True)
     tmp = LIB_PATH + ".tmp"
     # -ffp-contract=off: the restatement rounds each operation as written.
-    cmd = ["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-shared", "-fPIC", "-o", tmp, SRC, REF_SRC, "-ldl",
-           "-lpthread", "-lm"]
+    cmd = ["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-shared", "-fPIC", "-o", tmp, SRC, REF_SRC, MODEL_SRC,
+           "-ldl", "-lpthread", "-lm"]
     subprocess.run(cmd, check=True, capture_output=True)
     os.replace(tmp, LIB_PATH)
     return LIB_PATH
@@ -83,6 +84,7 @@ def _load():
             ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
         lib.ref_zgeev_batched.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.c_void_p]
+        lib.model_zgeev_batched.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 5
         st = lib.cpu_zgeev_open(find_lapack().encode())
         if st != 0:
             raise RuntimeError(f"cannot open LAPACK ({st})")
@@ -196,6 +198,25 @@ def reference_algorithm(A: np.ndarray):
     flag = np.empty(b, np.int32)
     lib.ref_zgeev_batched(n, b, A.ctypes.data, w.ctypes.data, flag.ctypes.data)
     return w, flag
+
+
+def model_qr(A: np.ndarray, est: np.ndarray | None = None):
+    """CPU model of this library's own iteration (oracle/model_qr.c): Householder
+    Hessenberg, then single-shift QR with Ahues-Tisseur deflation, Wilkinson and ad hoc
+    shifts and, given ``est`` (complex64 ``[batch, n]``), the nearest unused estimate as
+    the first shift after each deflation. Returns ``(w, flag, sweeps)`` per matrix."""
+    lib = _load()
+    A = _as_batch(A)
+    b, n, _ = A.shape
+    w = np.empty((b, n), np.complex128)
+    flag = np.empty(b, np.int32)
+    sweeps = np.empty(b, np.int64)
+    e = None
+    if est is not None:
+        e = np.ascontiguousarray(est, dtype=np.complex64).reshape(b, n)
+    lib.model_zgeev_batched(n, b, A.ctypes.data, w.ctypes.data, None if e is None else e.ctypes.data,
+                            flag.ctypes.data, sweeps.ctypes.data)
+    return w, flag, sweeps
 
 
 def matched_abs_errors(w_test: np.ndarray, w_ref: np.ndarray) -> np.ndarray:

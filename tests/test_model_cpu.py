@@ -1,0 +1,42 @@
+"""CPU model of this library's own iteration (oracle/model_qr.c): its
+eigenvalues agree with LAPACK, and it gives the sweep counts per eigenvalue
+quoted for the FP32 shift hints (Wilkinson shifts only; hints of FP32
+accuracy; hints accurate to FP32 rounding)."""
+import numpy as np
+import pytest
+
+from oracle import lapack_oracle as lo
+from tokura_zgeev_batched_gb300 import workloads as wl
+
+
+@pytest.mark.parametrize("gen", ["gaussian", "companion", "vdv"])
+@pytest.mark.parametrize("n", [1, 2, 5, 16, 64])
+def test_model_agrees_with_lapack(gen, n):
+    A = wl.GENERATORS[gen](12, n, seed=40 + n)
+    w_ref, info, _ = lo.zgeev(A, threads=2)
+    w, flag, _ = lo.model_qr(A)
+    assert (flag == 0).all() and (info == 0).all()
+    fro = np.maximum(np.linalg.norm(A, axis=(1, 2)), 1e-300)
+    _, rc, _ = lo.zgeevx_rconde(A, threads=2)
+    well = (1.0 / np.maximum(rc, 1e-300)).max(axis=1) <= lo.COND_MAX
+    err = lo.matched_abs_errors(w, w_ref).max(axis=1) / fro
+    assert np.all(err[well] <= lo.TOL_REL_FRO), err
+
+
+def test_model_sweeps_per_eigenvalue_with_and_without_hints():
+    import scipy.linalg.lapack as lapack
+
+    n, b = 64, 16
+    A = wl.gaussian(b, n, seed=7)
+    w_ref = lo.zgeev(A, threads=2)[0]
+    # FP32 eigenvalues of the same matrices (the library reads A[k] column-major: A[k].T).
+    fp32 = np.stack([lapack.cgeev(A[k].T.astype(np.complex64), compute_vl=0, compute_vr=0)[0] for k in range(b)])
+    per_eig = {}
+    for tag, est in (("wilkinson", None), ("fp32", fp32), ("rounded", w_ref.astype(np.complex64))):
+        w, flag, sweeps = lo.model_qr(A, est)
+        assert (flag == 0).all()
+        assert lo.matched_abs_errors(w, w_ref).max() <= lo.TOL_REL_FRO * np.linalg.norm(A, axis=(1, 2)).min()
+        per_eig[tag] = sweeps.sum() / (b * n)
+    assert 3.1 <= per_eig["wilkinson"] <= 3.6, per_eig
+    assert 2.3 <= per_eig["fp32"] <= 2.9, per_eig
+    assert 1.8 <= per_eig["rounded"] <= 2.3, per_eig
