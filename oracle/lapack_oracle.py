@@ -85,6 +85,8 @@ def _load():
         lib.ref_zgeev_batched.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.c_void_p]
         lib.model_zgeev_batched.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 5
+        lib.model_estimates_batched.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                                ctypes.c_float]
         st = lib.cpu_zgeev_open(find_lapack().encode())
         if st != 0:
             raise RuntimeError(f"cannot open LAPACK ({st})")
@@ -217,6 +219,17 @@ def model_qr(A: np.ndarray, est: np.ndarray | None = None):
     lib.model_zgeev_batched(n, b, A.ctypes.data, w.ctypes.data, None if e is None else e.ctypes.data,
                             flag.ctypes.data, sweeps.ctypes.data)
     return w, flag, sweeps
+
+
+def model_estimates(A: np.ndarray, tol: float = 1e-5) -> np.ndarray:
+    """CPU model of the FP32 estimator (oracle/model_qr.c): complex64 ``[batch, n]``
+    estimates with deflation tolerance ``tol`` (the library uses 1e-5)."""
+    lib = _load()
+    A = _as_batch(A)
+    b, n, _ = A.shape
+    est = np.empty((b, n), np.complex64)
+    lib.model_estimates_batched(n, b, A.ctypes.data, est.ctypes.data, float(tol))
+    return est
 
 
 def matched_abs_errors(w_test: np.ndarray, w_ref: np.ndarray) -> np.ndarray:

@@ -206,6 +206,189 @@ static int qr(int n, zc* a, zc* w, const float* est, unsigned char* used, long* 
   }
 }
 
+/* ---- FP32 estimator (csrc/zgeev_estimate.cuh: hessenberg_f, qr_estimates,
+ * estimate_matrix): the same reduction and iteration in single precision on
+ * the matrix scaled by a power of two to entries below 2 in magnitude, with
+ * deflation relative to `tol` instead of the ulp and a cap of 30 sweeps per
+ * eigenvalue (the diagonal then serves as estimates). */
+
+typedef struct { float re, im; } fc;
+
+static fc f2(float r, float i) { fc v = {r, i}; return v; }
+static fc fadd(fc a, fc b) { return f2(a.re + b.re, a.im + b.im); }
+static fc fsub(fc a, fc b) { return f2(a.re - b.re, a.im - b.im); }
+static fc fmul(fc a, fc b) { return f2(a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re); }
+static fc fconj(fc a) { return f2(a.re, -a.im); }
+static fc fscl(fc a, float s) { return f2(a.re * s, a.im * s); }
+static float fabs1(fc a) { return fabsf(a.re) + fabsf(a.im); }
+static float fabs2(fc a) { return a.re * a.re + a.im * a.im; }
+
+#define S(r, c) h[(size_t)(c) * n + (r)]
+
+static void hessenberg_f(int n, fc* h, fc* v) {
+  for (int r = 0; r + 2 < n; ++r) {
+    int m = n - r - 1;
+    float s2 = 0.0f;
+    for (int i = 1; i < m; ++i) s2 += fabs2(S(r + 1 + i, r));
+    if (s2 == 0.0f) continue;
+    fc x0 = S(r + 1, r);
+    float a0sq = fabs2(x0), tot = a0sq + s2, xn = sqrtf(tot), tau;
+    fc alpha, cg;
+    if (a0sq > 0.0f) {
+      float a0 = sqrtf(a0sq), d = a0 + xn, ig = 1.0f / (a0 * d);
+      cg = f2(x0.re * ig, -x0.im * ig);
+      alpha = fscl(x0, -xn / a0);
+      tau = d / xn;
+    } else {
+      cg = f2(1.0f / xn, 0.0f);
+      alpha = f2(-xn, 0.0f);
+      tau = 1.0f;
+    }
+    v[0] = f2(1.0f, 0.0f);
+    for (int i = 1; i < m; ++i) v[i] = fmul(S(r + 1 + i, r), cg);
+    S(r + 1, r) = alpha;
+    for (int i = 1; i < m; ++i) S(r + 1 + i, r) = f2(0.0f, 0.0f);
+    for (int c = r + 1; c < n; ++c) {
+      fc w = f2(0.0f, 0.0f);
+      for (int i = 0; i < m; ++i) w = fadd(w, fmul(fconj(v[i]), S(r + 1 + i, c)));
+      w = fscl(w, tau);
+      for (int i = 0; i < m; ++i) S(r + 1 + i, c) = fsub(S(r + 1 + i, c), fmul(v[i], w));
+    }
+    for (int q = 0; q < n; ++q) {
+      fc w = f2(0.0f, 0.0f);
+      for (int i = 0; i < m; ++i) w = fadd(w, fmul(S(q, r + 1 + i), v[i]));
+      w = fscl(w, tau);
+      for (int i = 0; i < m; ++i) S(q, r + 1 + i) = fsub(S(q, r + 1 + i), fmul(w, fconj(v[i])));
+    }
+  }
+}
+
+static int negligible_f(int n, const fc* h, int k, int lo, int hi, float smlnum, float tol) {
+  float h1 = fabs1(S(k, k - 1));
+  if (h1 <= smlnum) return 1;
+  fc dkk = S(k, k), dk1 = S(k - 1, k - 1);
+  float tst = fabs1(dk1) + fabs1(dkk);
+  if (tst == 0.0f) {
+    if (k - 2 >= lo) tst += fabs1(S(k - 1, k - 2));
+    if (k + 1 <= hi) tst += fabs1(S(k + 1, k));
+  }
+  if (h1 > tol * tst) return 0;
+  float hu = fabs1(S(k - 1, k));
+  float ab = fmaxf(h1, hu), ba = fminf(h1, hu);
+  float dd = fabs1(fsub(dk1, dkk)), d1 = fabs1(dkk);
+  float aa = fmaxf(d1, dd), bb = fminf(d1, dd), sum = aa + ab;
+  return ba * (ab / sum) <= fmaxf(smlnum, tol * (bb * (aa / sum)));
+}
+
+static fc wilkinson_f(fc a, fc b, fc c, fc d) {
+  fc bc = fmul(b, c);
+  if (bc.re == 0.0f && bc.im == 0.0f) return d;
+  fc x = fscl(fsub(a, d), 0.5f);
+  float sc = fmaxf(fabs1(x), sqrtf(fabs1(bc)));
+  if (!(sc > 0.0f) || !(sc < 3.0e38f)) return d;
+  fc xs = fscl(x, 1.0f / sc), bcs = fscl(bc, 1.0f / (sc * sc));
+  fc zz = fadd(fmul(xs, xs), bcs);
+  float m = hypotf(zz.re, zz.im);
+  fc y = f2(0.0f, 0.0f);
+  if (m > 0.0f) {
+    float t = sqrtf(0.5f * (m + fabsf(zz.re))), hh = zz.im / (2.0f * t);
+    y = zz.re >= 0.0f ? f2(t, hh) : f2(fabsf(hh), copysignf(t, zz.im));
+  }
+  if (xs.re * y.re + xs.im * y.im < 0.0f) y = f2(-y.re, -y.im);
+  fc den = fadd(xs, y);
+  float dd = fabs2(den);
+  if (!(dd > 0.0f)) return d;
+  fc corr = f2((bcs.re * den.re + bcs.im * den.im) / dd, (bcs.im * den.re - bcs.re * den.im) / dd);
+  return fsub(d, fscl(corr, sc));
+}
+
+static void rot_f(fc x, fc y, float* c, fc* s, fc* r) {
+  float p = fabs2(x), q = fabs2(y), nn = p + q;
+  if (q == 0.0f) {
+    *c = 1.0f; *s = f2(0.0f, 0.0f); *r = x;
+  } else if (p * nn < 1e-30f) {
+    float iq = 1.0f / sqrtf(q);
+    *c = 0.0f; *s = fscl(fconj(y), iq); *r = f2(q * iq, 0.0f);
+  } else {
+    float R = 1.0f / sqrtf(p * nn);
+    *c = p * R; *s = fscl(fmul(x, fconj(y)), R); *r = fscl(x, nn * R);
+  }
+}
+
+static void qr_f(int n, fc* h, float* est, float f, float tol) {
+  const float smlnum = 1.1754943508222875e-38f * ((float)n / 5.9604644775390625e-08f);
+  int i = n - 1, lo = 0, its = 0, kdefl = 0;
+  for (;;) {
+    for (;;) {
+      int hit = lo;
+      for (int k = i; k > lo; --k)
+        if (negligible_f(n, h, k, lo, i, smlnum, tol)) { hit = k; break; }
+      lo = hit;
+      if (lo < i) break;
+      est[2 * i] = S(i, i).re * f;
+      est[2 * i + 1] = S(i, i).im * f;
+      i -= 1; lo = 0; its = 0; kdefl = 0;
+      if (i < 0) return;
+    }
+    if (its >= 30) {
+      for (int k = 0; k <= i; ++k) { est[2 * k] = S(k, k).re * f; est[2 * k + 1] = S(k, k).im * f; }
+      return;
+    }
+    ++its; ++kdefl;
+    fc sigma;
+    if (kdefl % (2 * kPeriod) == 0) sigma = f2(S(i, i).re + 0.75f * fabs1(S(i, i - 1)), S(i, i).im);
+    else if (kdefl % kPeriod == 0) sigma = f2(S(lo, lo).re + 0.75f * fabs1(S(lo + 1, lo)), S(lo, lo).im);
+    else sigma = wilkinson_f(S(i - 1, i - 1), S(i - 1, i), S(i, i - 1), S(i, i));
+    for (int j = lo; j < i; ++j) {
+      fc x, y, r, s;
+      float c;
+      if (j == lo) { x = fsub(S(lo, lo), sigma); y = S(lo + 1, lo); }
+      else { x = S(j, j - 1); y = S(j + 1, j - 1); }
+      rot_f(x, y, &c, &s, &r);
+      if (j > lo) { S(j, j - 1) = r; S(j + 1, j - 1) = f2(0.0f, 0.0f); }
+      for (int col = j; col <= i; ++col) {
+        fc p = S(j, col), q = S(j + 1, col);
+        S(j, col) = fadd(fscl(p, c), fmul(s, q));
+        S(j + 1, col) = fsub(fscl(q, c), fmul(fconj(s), p));
+      }
+      int qend = j + 2 < i ? j + 2 : i;
+      for (int row = lo; row <= qend; ++row) {
+        fc p = S(row, j), q = S(row, j + 1);
+        S(row, j) = fadd(fscl(p, c), fmul(fconj(s), q));
+        S(row, j + 1) = fsub(fscl(q, c), fmul(s, p));
+      }
+    }
+  }
+}
+
+/* FP32 estimates of every matrix of the batch (2n floats per matrix), as the
+ * GPU estimator computes them, with deflation tolerance `tol` (1e-5 there). */
+void model_estimates_batched(int n, int batch, const double* A, float* est, float tol) {
+  fc* h = malloc(sizeof(fc) * (size_t)n * n);
+  fc* v = malloc(sizeof(fc) * (size_t)n);
+  for (int j = 0; j < batch; ++j) {
+    const double* src = A + (size_t)j * 2 * n * n;
+    double amax = 0.0;
+    for (size_t e = 0; e < (size_t)2 * n * n; ++e) amax = fmax(amax, fabs(src[e]));
+    float* out = est + (size_t)j * 2 * n;
+    if (amax == 0.0 || !isfinite(amax)) {
+      for (int i = 0; i < 2 * n; ++i) out[i] = 0.0f;
+      continue;
+    }
+    int top;
+    frexp(amax, &top);
+    top -= 1; /* amax in [2^top, 2^(top+1)) */
+    double sc = ldexp(1.0, -top);
+    for (size_t e = 0; e < (size_t)n * n; ++e) h[e] = f2((float)(src[2 * e] * sc), (float)(src[2 * e + 1] * sc));
+    hessenberg_f(n, h, v);
+    qr_f(n, h, out, (float)ldexp(1.0, top), tol);
+  }
+  free(h);
+  free(v);
+}
+
+#undef S
+
 /* Batch driver: A and w as in the oracle (column-major buffers, w[j*n + i]);
  * est: NULL or 2n floats per matrix; flag and sweeps per matrix. */
 void model_zgeev_batched(int n, int batch, const double* A, double* w, const float* est, int* flag, long* sweeps) {

@@ -2,12 +2,12 @@
 //
 // GB300 runs FP32 about 60x faster than FP64, so a complete FP32 eigenvalue
 // computation costs a few percent of the FP64 one. Its eigenvalues (relative
-// accuracy ~1e-7 for well-conditioned ones) are handed to the FP64 QR, which
-// uses the nearest unused estimate as the shift of the first sweep after each
-// deflation: that sweep already brings the bottom subdiagonal down by ~1e-7,
-// and the Wilkinson sweep after it finishes the eigenvalue, ~2.1 sweeps per
-// eigenvalue instead of ~3.4 with Wilkinson shifts alone (CPU model of both
-// iterations on complex Gaussian matrices, n = 32 and 64). The estimates only
+// accuracy ~1e-6, set by FP32's backward error) are handed to the FP64 QR,
+// which uses the nearest unused estimate as the shift of the first sweep after
+// each deflation: that sweep brings the bottom subdiagonal down by about the
+// estimate's error and one or two Wilkinson sweeps finish the eigenvalue,
+// ~2.65 sweeps per eigenvalue instead of ~3.37 with Wilkinson shifts alone
+// (CPU model of both iterations, oracle/model_qr.c, complex Gaussian, n = 64). The estimates only
 // steer the iteration; the FP64 result and its accuracy come from the FP64
 // QR as before, and a bad or missing estimate costs at most one sweep.
 //
