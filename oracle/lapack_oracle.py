@@ -85,6 +85,7 @@ def _load():
         lib.ref_zgeev_batched.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.c_void_p]
         lib.model_zgeev_batched.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 5
+        lib.model_zgeev_batched_opts.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 6 + [ctypes.c_int]
         lib.model_estimates_batched.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                                 ctypes.c_float]
         st = lib.cpu_zgeev_open(find_lapack().encode())
@@ -219,6 +220,25 @@ def model_qr(A: np.ndarray, est: np.ndarray | None = None):
     lib.model_zgeev_batched(n, b, A.ctypes.data, w.ctypes.data, None if e is None else e.ctypes.data,
                             flag.ctypes.data, sweeps.ctypes.data)
     return w, flag, sweeps
+
+
+def model_qr_variant(A: np.ndarray, est: np.ndarray | None = None, start_row: bool = False,
+                     estimate_twice: bool = False):
+    """model_qr with the variants the library does not use (zlahqr's start-row search;
+    the estimate as the shift of the second sweep too). Returns ``(w, flag, sweeps, work)``,
+    work = element-pair rotation updates per matrix."""
+    lib = _load()
+    A = _as_batch(A)
+    b, n, _ = A.shape
+    w = np.empty((b, n), np.complex128)
+    flag = np.empty(b, np.int32)
+    sweeps = np.empty(b, np.int64)
+    work = np.empty(b, np.int64)
+    e = None if est is None else np.ascontiguousarray(est, dtype=np.complex64).reshape(b, n)
+    lib.model_zgeev_batched_opts(n, b, A.ctypes.data, w.ctypes.data, None if e is None else e.ctypes.data,
+                                 flag.ctypes.data, sweeps.ctypes.data, work.ctypes.data,
+                                 int(start_row) | (2 if estimate_twice else 0))
+    return w, flag, sweeps, work
 
 
 def model_estimates(A: np.ndarray, tol: float = 1e-5) -> np.ndarray:

@@ -144,9 +144,14 @@ static int nearest(const float* est, int n, const unsigned char* used, zc t) {
 
 /* Single-shift QR, bottom up, one sweep per loop iteration, updates restricted
  * to the active block. est (2n floats or NULL): the nearest unused estimate
- * is the shift of the first sweep after each deflation. Returns the flag (0
- * converged, 1 sweep cap hit) and adds the sweeps made to *sweeps. */
-static int qr(int n, zc* a, zc* w, const float* est, unsigned char* used, long* sweeps) {
+ * is the shift of the first sweep after each deflation. options (variants
+ * the library does not use, kept to measure them): bit 0 begins each sweep
+ * below two consecutive small subdiagonals when allowed (the published
+ * zlahqr start-row test); bit 1 takes the estimate for the second sweep too.
+ * Returns the flag (0 converged, 1 sweep cap hit) and adds the sweeps made to
+ * *sweeps and the element-pair rotation updates to *work. */
+static int qr(int n, zc* a, zc* w, const float* est, unsigned char* used, long* sweeps, long long* work,
+              int options) {
   double smlnum = kSafeMin * ((double)n / kUlp);
   int itmax = 30 * (n > 10 ? n : 10);
   int i = n - 1, lo = 0, its = 0, kdefl = 0;
@@ -179,18 +184,32 @@ static int qr(int n, zc* a, zc* w, const float* est, unsigned char* used, long* 
       sigma = z(H(lo, lo).re + kWeight * zabs1(H(lo + 1, lo)), H(lo, lo).im);
     } else {
       sigma = wilkinson(H(i - 1, i - 1), H(i - 1, i), H(i, i - 1), H(i, i));
-      if (est && its == 1) {
+      if (est && (its == 1 || ((options & 2) && its == 2))) {
         int k = nearest(est, n, used, sigma);
         if (k >= 0) sigma = z(est[2 * k], est[2 * k + 1]);
       }
     }
-    for (int j = lo; j < i; ++j) {
+    int start = lo;
+    if (options & 1) {
+      for (int m = i - 1; m > lo; --m) {
+        zc h11 = H(m, m), h22 = H(m + 1, m + 1), h11s = zsub(h11, sigma), h21 = H(m + 1, m);
+        double sc = zabs1(h11s) + zabs1(h21);
+        if (!(sc > 0.0)) continue;
+        if (zabs1(H(m, m - 1)) * (zabs1(h21) / sc) <= kUlp * (zabs1(zscale(h11s, 1.0 / sc)) * (zabs1(h11) + zabs1(h22)))) {
+          start = m;
+          break;
+        }
+      }
+    }
+    for (int j = start; j < i; ++j) {
       zc x, y, r, s;
       double c;
-      if (j == lo) { x = zsub(H(lo, lo), sigma); y = H(lo + 1, lo); }
+      if (j == start) { x = zsub(H(start, start), sigma); y = H(start + 1, start); }
       else { x = H(j, j - 1); y = H(j + 1, j - 1); }
       make_rot(x, y, &c, &s, &r);
-      if (j > lo) { H(j, j - 1) = r; H(j + 1, j - 1) = z(0.0, 0.0); }
+      if (j > start) { H(j, j - 1) = r; H(j + 1, j - 1) = z(0.0, 0.0); }
+      else if (start > lo) H(start, start - 1) = zscale(H(start, start - 1), c); /* the fill-in below is negligible */
+      *work += (i - j + 1) + ((j + 2 < i ? j + 2 : i) - lo + 1);
       for (int col = j; col <= i; ++col) { /* rows j, j+1 */
         zc p = H(j, col), q = H(j + 1, col);
         H(j, col) = zadd(zscale(p, c), zmul(s, q));
@@ -391,7 +410,8 @@ void model_estimates_batched(int n, int batch, const double* A, float* est, floa
 
 /* Batch driver: A and w as in the oracle (column-major buffers, w[j*n + i]);
  * est: NULL or 2n floats per matrix; flag and sweeps per matrix. */
-void model_zgeev_batched(int n, int batch, const double* A, double* w, const float* est, int* flag, long* sweeps) {
+void model_zgeev_batched_opts(int n, int batch, const double* A, double* w, const float* est, int* flag, long* sweeps,
+                              long long* work, int options) {
   zc* a = malloc(sizeof(zc) * (size_t)n * n);
   zc* v = malloc(sizeof(zc) * (size_t)n);
   unsigned char* used = malloc((size_t)n);
@@ -400,9 +420,17 @@ void model_zgeev_batched(int n, int batch, const double* A, double* w, const flo
     for (size_t e = 0; e < (size_t)n * n; ++e) a[e] = z(src[2 * e], src[2 * e + 1]);
     hessenberg(n, a, v);
     sweeps[j] = 0;
-    flag[j] = qr(n, a, (zc*)(w + (size_t)j * 2 * n), est ? est + (size_t)j * 2 * n : NULL, used, &sweeps[j]);
+    work[j] = 0;
+    flag[j] = qr(n, a, (zc*)(w + (size_t)j * 2 * n), est ? est + (size_t)j * 2 * n : NULL, used, &sweeps[j],
+                 &work[j], options);
   }
   free(a);
   free(v);
   free(used);
+}
+
+void model_zgeev_batched(int n, int batch, const double* A, double* w, const float* est, int* flag, long* sweeps) {
+  long long* work = malloc(sizeof(long long) * (size_t)(batch > 0 ? batch : 1));
+  model_zgeev_batched_opts(n, batch, A, w, est, flag, sweeps, work, 0);
+  free(work);
 }

@@ -58,3 +58,24 @@ def test_model_estimator_accuracy_and_tolerance():
         assert (flag == 0).all()
         sweeps[tol] = sw.sum() / (b * n)
     assert 2.3 <= sweeps[1e-5] <= 2.9 and abs(sweeps[1e-5] - sweeps[5.9604644775390625e-08]) < 0.15, sweeps
+
+
+def test_model_variants_not_adopted():
+    """The two shift-strategy variants the library does not use: zlahqr's start-row search
+    saves only a few percent of the rotation work; the estimate as the second sweep's shift
+    costs sweeps."""
+    n, b = 64, 16
+    A = wl.gaussian(b, n, seed=13)
+    w_ref = lo.zgeev(A, threads=2)[0]
+    est = lo.model_estimates(A)
+    base = lo.model_qr_variant(A, est)
+    start = lo.model_qr_variant(A, est, start_row=True)
+    twice = lo.model_qr_variant(A, est, estimate_twice=True)
+    for w, flag, _, _ in (base, start, twice):
+        assert (flag == 0).all()
+        assert lo.matched_abs_errors(w, w_ref).max() <= lo.TOL_REL_FRO * np.linalg.norm(A, axis=(1, 2)).min()
+    saving = 1.0 - start[3].sum() / base[3].sum()
+    assert 0.0 <= saving < 0.06, saving
+    assert twice[2].sum() > 1.05 * base[2].sum()
+    w0, f0, s0 = lo.model_qr(A, est)
+    assert np.array_equal(s0, base[2]) and np.array_equal(w0.view(np.uint64), base[0].view(np.uint64))
