@@ -87,7 +87,7 @@ def _load():
         lib.model_zgeev_batched.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 5
         lib.model_zgeev_batched_opts.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 6 + [ctypes.c_int]
         lib.model_estimates_batched.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
-                                                ctypes.c_float]
+                                                ctypes.c_float, ctypes.c_void_p]
         st = lib.cpu_zgeev_open(find_lapack().encode())
         if st != 0:
             raise RuntimeError(f"cannot open LAPACK ({st})")
@@ -241,15 +241,17 @@ def model_qr_variant(A: np.ndarray, est: np.ndarray | None = None, start_row: bo
     return w, flag, sweeps, work
 
 
-def model_estimates(A: np.ndarray, tol: float = 1e-5) -> np.ndarray:
+def model_estimates(A: np.ndarray, tol: float = 1e-5, return_sweeps: bool = False):
     """CPU model of the FP32 estimator (oracle/model_qr.c): complex64 ``[batch, n]``
-    estimates with deflation tolerance ``tol`` (the library uses 1e-5)."""
+    estimates with deflation tolerance ``tol`` (the library uses 1e-5); with
+    ``return_sweeps`` also the FP32 QR's sweeps per matrix."""
     lib = _load()
     A = _as_batch(A)
     b, n, _ = A.shape
     est = np.empty((b, n), np.complex64)
-    lib.model_estimates_batched(n, b, A.ctypes.data, est.ctypes.data, float(tol))
-    return est
+    sweeps = np.empty(b, np.int64)
+    lib.model_estimates_batched(n, b, A.ctypes.data, est.ctypes.data, float(tol), sweeps.ctypes.data)
+    return (est, sweeps) if return_sweeps else est
 
 
 def matched_abs_errors(w_test: np.ndarray, w_ref: np.ndarray) -> np.ndarray:

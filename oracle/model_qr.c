@@ -334,7 +334,7 @@ static void rot_f(fc x, fc y, float* c, fc* s, fc* r) {
   }
 }
 
-static void qr_f(int n, fc* h, float* est, float f, float tol) {
+static void qr_f(int n, fc* h, float* est, float f, float tol, long* sweeps) {
   const float smlnum = 1.1754943508222875e-38f * ((float)n / 5.9604644775390625e-08f);
   int i = n - 1, lo = 0, its = 0, kdefl = 0;
   for (;;) {
@@ -353,7 +353,7 @@ static void qr_f(int n, fc* h, float* est, float f, float tol) {
       for (int k = 0; k <= i; ++k) { est[2 * k] = S(k, k).re * f; est[2 * k + 1] = S(k, k).im * f; }
       return;
     }
-    ++its; ++kdefl;
+    ++its; ++kdefl; ++*sweeps;
     fc sigma;
     if (kdefl % (2 * kPeriod) == 0) sigma = f2(S(i, i).re + 0.75f * fabs1(S(i, i - 1)), S(i, i).im);
     else if (kdefl % kPeriod == 0) sigma = f2(S(lo, lo).re + 0.75f * fabs1(S(lo + 1, lo)), S(lo, lo).im);
@@ -381,8 +381,9 @@ static void qr_f(int n, fc* h, float* est, float f, float tol) {
 }
 
 /* FP32 estimates of every matrix of the batch (2n floats per matrix), as the
- * GPU estimator computes them, with deflation tolerance `tol` (1e-5 there). */
-void model_estimates_batched(int n, int batch, const double* A, float* est, float tol) {
+ * GPU estimator computes them, with deflation tolerance `tol` (1e-5 there);
+ * sweeps (NULL or one per matrix): the FP32 QR's sweeps. */
+void model_estimates_batched(int n, int batch, const double* A, float* est, float tol, long* sweeps) {
   fc* h = malloc(sizeof(fc) * (size_t)n * n);
   fc* v = malloc(sizeof(fc) * (size_t)n);
   for (int j = 0; j < batch; ++j) {
@@ -390,6 +391,9 @@ void model_estimates_batched(int n, int batch, const double* A, float* est, floa
     double amax = 0.0;
     for (size_t e = 0; e < (size_t)2 * n * n; ++e) amax = fmax(amax, fabs(src[e]));
     float* out = est + (size_t)j * 2 * n;
+    long dummy = 0;
+    long* sw = sweeps ? &sweeps[j] : &dummy;
+    *sw = 0;
     if (amax == 0.0 || !isfinite(amax)) {
       for (int i = 0; i < 2 * n; ++i) out[i] = 0.0f;
       continue;
@@ -400,7 +404,7 @@ void model_estimates_batched(int n, int batch, const double* A, float* est, floa
     double sc = ldexp(1.0, -top);
     for (size_t e = 0; e < (size_t)n * n; ++e) h[e] = f2((float)(src[2 * e] * sc), (float)(src[2 * e + 1] * sc));
     hessenberg_f(n, h, v);
-    qr_f(n, h, out, (float)ldexp(1.0, top), tol);
+    qr_f(n, h, out, (float)ldexp(1.0, top), tol, sw);
   }
   free(h);
   free(v);

@@ -49,15 +49,18 @@ def test_model_estimator_accuracy_and_tolerance():
     n, b = 64, 16
     A = wl.gaussian(b, n, seed=11)
     w_ref = lo.zgeev(A, threads=2)[0]
-    sweeps = {}
+    sweeps, fp32_sweeps = {}, {}
     for tol in (5.9604644775390625e-08, 1e-5):
-        est = lo.model_estimates(A, tol)
+        est, sw32 = lo.model_estimates(A, tol, return_sweeps=True)
+        fp32_sweeps[tol] = sw32.sum() / (b * n)
         rel = lo.matched_abs_errors(est.astype(np.complex128), w_ref) / np.abs(w_ref)
         assert np.median(rel) < 3e-6 and rel.max() < 1e-3, (tol, np.median(rel), rel.max())
         w, flag, sw = lo.model_qr(A, est)
         assert (flag == 0).all()
         sweeps[tol] = sw.sum() / (b * n)
     assert 2.3 <= sweeps[1e-5] <= 2.9 and abs(sweeps[1e-5] - sweeps[5.9604644775390625e-08]) < 0.15, sweeps
+    # the tolerance's point: the FP32 QR itself stops ~0.3 sweeps per eigenvalue earlier
+    assert fp32_sweeps[1e-5] < fp32_sweeps[5.9604644775390625e-08] - 0.2, fp32_sweeps
 
 
 def test_model_variants_not_adopted():
