@@ -82,8 +82,9 @@ static void hessenberg(int n, zc* a, zc* v) {
   }
 }
 
-/* Ahues-Tisseur deflation test of subdiagonal entry k of the block [lo, hi]. */
-static int negligible(int n, const zc* a, int k, int lo, int hi, double smlnum) {
+/* Ahues-Tisseur deflation test of subdiagonal entry k of the block [lo, hi],
+ * relative to tol (the ulp for eigenvalues; 100 ulp in the gradient's QR). */
+static int negligible(int n, const zc* a, int k, int lo, int hi, double smlnum, double tol) {
   zc hk = H(k, k - 1);
   double h1 = zabs1(hk);
   if (h1 <= smlnum) return 1;
@@ -93,12 +94,12 @@ static int negligible(int n, const zc* a, int k, int lo, int hi, double smlnum) 
     if (k - 2 >= lo) tst += zabs1(H(k - 1, k - 2));
     if (k + 1 <= hi) tst += zabs1(H(k + 1, k));
   }
-  if (h1 > kUlp * tst) return 0;
+  if (h1 > tol * tst) return 0;
   double hu = zabs1(H(k - 1, k));
   double ab = fmax(h1, hu), ba = fmin(h1, hu);
   double dd = zabs1(zsub(dk1, dkk)), d1 = zabs1(dkk);
   double aa = fmax(d1, dd), bb = fmin(d1, dd), s = aa + ab;
-  return ba * (ab / s) <= fmax(smlnum, kUlp * (bb * (aa / s)));
+  return ba * (ab / s) <= fmax(smlnum, tol * (bb * (aa / s)));
 }
 
 /* Eigenvalue of [[a, b], [c, d]] nearer to d, in a scaled form. */
@@ -129,6 +130,18 @@ static void make_rot(zc x, zc y, double* c, zc* s, zc* r) {
   }
 }
 
+/* Index of the unused FP64 value nearest to t, or -1 (the gradient's QR). */
+static int nearest64(const double* lam, int n, const unsigned char* used, zc t) {
+  double best = INFINITY;
+  int kb = -1;
+  for (int k = 0; k < n; ++k) {
+    if (used[k]) continue;
+    double dx = lam[2 * k] - t.re, dy = lam[2 * k + 1] - t.im, d2 = dx * dx + dy * dy;
+    if (d2 < best) { best = d2; kb = k; }
+  }
+  return kb;
+}
+
 /* Index of the unused estimate nearest to t (FP32 distances), or -1. */
 static int nearest(const float* est, int n, const unsigned char* used, zc t) {
   float tx = (float)t.re, ty = (float)t.im, best = 3.0e38f;
@@ -148,10 +161,13 @@ static int nearest(const float* est, int n, const unsigned char* used, zc t) {
  * the library does not use, kept to measure them): bit 0 begins each sweep
  * below two consecutive small subdiagonals when allowed (the published
  * zlahqr start-row test); bit 1 takes the estimate for the second sweep too.
+ * lam (2n doubles or NULL) and tol model the gradient's Schur iteration
+ * (zgeev_backward.cuh: schur_qr): the nearest unused forward eigenvalue is
+ * the first shift after each deflation, deflating at tol instead of the ulp.
  * Returns the flag (0 converged, 1 sweep cap hit) and adds the sweeps made to
  * *sweeps and the element-pair rotation updates to *work. */
-static int qr(int n, zc* a, zc* w, const float* est, unsigned char* used, long* sweeps, long long* work,
-              int options) {
+static int qr(int n, zc* a, zc* w, const float* est, const double* lam, double tol, unsigned char* used,
+              long* sweeps, long long* work, int options) {
   double smlnum = kSafeMin * ((double)n / kUlp);
   int itmax = 30 * (n > 10 ? n : 10);
   int i = n - 1, lo = 0, its = 0, kdefl = 0;
@@ -160,11 +176,14 @@ static int qr(int n, zc* a, zc* w, const float* est, unsigned char* used, long* 
     for (;;) {
       int hit = lo;
       for (int k = i; k > lo; --k)
-        if (negligible(n, a, k, lo, i, smlnum)) { hit = k; break; }
+        if (negligible(n, a, k, lo, i, smlnum, tol)) { hit = k; break; }
       lo = hit;
       if (lo < i) break;
       w[i] = H(i, i);
-      if (est) {
+      if (lam) {
+        int k = nearest64(lam, n, used, w[i]);
+        if (k >= 0) used[k] = 1;
+      } else if (est) {
         int k = nearest(est, n, used, w[i]);
         if (k >= 0) used[k] = 1;
       }
@@ -184,7 +203,10 @@ static int qr(int n, zc* a, zc* w, const float* est, unsigned char* used, long* 
       sigma = z(H(lo, lo).re + kWeight * zabs1(H(lo + 1, lo)), H(lo, lo).im);
     } else {
       sigma = wilkinson(H(i - 1, i - 1), H(i - 1, i), H(i, i - 1), H(i, i));
-      if (est && (its == 1 || ((options & 2) && its == 2))) {
+      if (lam && its == 1) {
+        int k = nearest64(lam, n, used, sigma);
+        if (k >= 0) sigma = z(lam[2 * k], lam[2 * k + 1]);
+      } else if (est && (its == 1 || ((options & 2) && its == 2))) {
         int k = nearest(est, n, used, sigma);
         if (k >= 0) sigma = z(est[2 * k], est[2 * k + 1]);
       }
@@ -414,8 +436,8 @@ void model_estimates_batched(int n, int batch, const double* A, float* est, floa
 
 /* Batch driver: A and w as in the oracle (column-major buffers, w[j*n + i]);
  * est: NULL or 2n floats per matrix; flag and sweeps per matrix. */
-void model_zgeev_batched_opts(int n, int batch, const double* A, double* w, const float* est, int* flag, long* sweeps,
-                              long long* work, int options) {
+void model_zgeev_batched_opts(int n, int batch, const double* A, double* w, const float* est, const double* lam,
+                              double tol, int* flag, long* sweeps, long long* work, int options) {
   zc* a = malloc(sizeof(zc) * (size_t)n * n);
   zc* v = malloc(sizeof(zc) * (size_t)n);
   unsigned char* used = malloc((size_t)n);
@@ -425,8 +447,8 @@ void model_zgeev_batched_opts(int n, int batch, const double* A, double* w, cons
     hessenberg(n, a, v);
     sweeps[j] = 0;
     work[j] = 0;
-    flag[j] = qr(n, a, (zc*)(w + (size_t)j * 2 * n), est ? est + (size_t)j * 2 * n : NULL, used, &sweeps[j],
-                 &work[j], options);
+    flag[j] = qr(n, a, (zc*)(w + (size_t)j * 2 * n), est ? est + (size_t)j * 2 * n : NULL,
+                 lam ? lam + (size_t)j * 2 * n : NULL, tol, used, &sweeps[j], &work[j], options);
   }
   free(a);
   free(v);
@@ -435,6 +457,6 @@ void model_zgeev_batched_opts(int n, int batch, const double* A, double* w, cons
 
 void model_zgeev_batched(int n, int batch, const double* A, double* w, const float* est, int* flag, long* sweeps) {
   long long* work = malloc(sizeof(long long) * (size_t)(batch > 0 ? batch : 1));
-  model_zgeev_batched_opts(n, batch, A, w, est, flag, sweeps, work, 0);
+  model_zgeev_batched_opts(n, batch, A, w, est, NULL, kUlp, flag, sweeps, work, 0);
   free(work);
 }

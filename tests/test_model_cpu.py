@@ -82,3 +82,23 @@ def test_model_variants_not_adopted():
     assert twice[2].sum() > 1.05 * base[2].sum()
     w0, f0, s0 = lo.model_qr(A, est)
     assert np.array_equal(s0, base[2]) and np.array_equal(w0.view(np.uint64), base[0].view(np.uint64))
+
+
+def test_model_gradient_schur_iteration():
+    """The gradient's Schur iteration (forward eigenvalues as first shifts, deflation at
+    100 ulp): about one sweep per eigenvalue, against ~1.7 at the ulp and ~3.1 with Wilkinson
+    shifts, with unchanged accuracy."""
+    ulp = 2.0 ** -52
+    n, b = 48, 24
+    A = wl.vdv(b, n, seed=5, min_sep=0.05)
+    w_ref = lo.zgeev(A, threads=2)[0]
+    fro = np.linalg.norm(A, axis=(1, 2))
+    per_eig = {}
+    for tag, lam, tol in (("wilkinson", None, ulp), ("perfect_ulp", w_ref, ulp), ("perfect_100ulp", w_ref, 100 * ulp)):
+        w, flag, sweeps, _ = lo.model_qr_variant(A, lam=lam, tol=tol)
+        assert (flag == 0).all()
+        assert (lo.matched_abs_errors(w, w_ref).max(axis=1) / fro).max() <= 1e-13
+        per_eig[tag] = sweeps.sum() / (b * n)
+    assert 2.8 <= per_eig["wilkinson"] <= 3.6, per_eig
+    assert 1.5 <= per_eig["perfect_ulp"] <= 2.0, per_eig
+    assert 0.8 <= per_eig["perfect_100ulp"] <= 1.2, per_eig
