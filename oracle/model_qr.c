@@ -3,13 +3,17 @@
  * Never linked into or called by the product library.
  *
  * Serial, one matrix at a time, column-major storage a[c*n + r], no
- * pre-scaling (inputs of moderate size). It restates the mathematics of the
- * GPU path (tokura_zgeev_batched_gb300/csrc/zgeev_lane.cuh: hessenberg,
- * negligible_subdiag, nearest_estimate, qr_eigenvalues; zgeev_device.cuh:
- * make_rot, wilkinson_shift) without its lane layout, so that tests can count
- * sweeps per eigenvalue with and without shift hints and compare eigenvalues
- * and flags with LAPACK. The reference's own algorithm is restated separately
- * (ref_algorithm.c).
+ * pre-scaling in the FP64 part (inputs of moderate size). It restates the
+ * mathematics of the GPU path without its lane layout:
+ *   - the FP64 eigenvalue iteration (tokura_zgeev_batched_gb300/csrc/
+ *     zgeev_lane.cuh: hessenberg, negligible_subdiag, nearest_estimate,
+ *     qr_eigenvalues; zgeev_device.cuh: make_rot, wilkinson_shift);
+ *   - the FP32 estimator (zgeev_estimate.cuh: hessenberg_f, qr_estimates);
+ *   - the eigenvalue part of the gradient's Schur iteration
+ *     (zgeev_backward.cuh: schur_qr, without Q or the vectors);
+ * so that tests can count sweeps per eigenvalue under each shift strategy and
+ * compare eigenvalues and flags with LAPACK. The reference's own algorithm is
+ * restated separately (ref_algorithm.c).
  */
 #include <math.h>
 #include <stdlib.h>
