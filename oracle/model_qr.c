@@ -168,10 +168,12 @@ static int nearest(const float* est, int n, const unsigned char* used, zc t) {
  * lam (2n doubles or NULL) and tol model the gradient's Schur iteration
  * (zgeev_backward.cuh: schur_qr): the nearest unused forward eigenvalue is
  * the first shift after each deflation, deflating at tol instead of the ulp.
+ * trace (NULL or trace_cap ints per matrix): the active window of each sweep,
+ * for simulating matrices that share a warp.
  * Returns the flag (0 converged, 1 sweep cap hit) and adds the sweeps made to
  * *sweeps and the element-pair rotation updates to *work. */
 static int qr(int n, zc* a, zc* w, const float* est, const double* lam, double tol, unsigned char* used,
-              long* sweeps, long long* work, int options) {
+              long* sweeps, long long* work, int options, int* trace, long trace_cap) {
   double smlnum = kSafeMin * ((double)n / kUlp);
   int itmax = 30 * (n > 10 ? n : 10);
   int i = n - 1, lo = 0, its = 0, kdefl = 0;
@@ -199,6 +201,7 @@ static int qr(int n, zc* a, zc* w, const float* est, const double* lam, double t
       for (int k = 0; k <= i; ++k) w[k] = H(k, k);
       return 1;
     }
+    if (trace && *sweeps < trace_cap) trace[*sweeps] = i - lo + 1; /* active window of this sweep */
     ++its; ++kdefl; ++*sweeps;
     zc sigma;
     if (kdefl % (2 * kPeriod) == 0) {
@@ -441,7 +444,8 @@ void model_estimates_batched(int n, int batch, const double* A, float* est, floa
 /* Batch driver: A and w as in the oracle (column-major buffers, w[j*n + i]);
  * est: NULL or 2n floats per matrix; flag and sweeps per matrix. */
 void model_zgeev_batched_opts(int n, int batch, const double* A, double* w, const float* est, const double* lam,
-                              double tol, int* flag, long* sweeps, long long* work, int options) {
+                              double tol, int* flag, long* sweeps, long long* work, int options, int* trace,
+                              long trace_cap) {
   zc* a = malloc(sizeof(zc) * (size_t)n * n);
   zc* v = malloc(sizeof(zc) * (size_t)n);
   unsigned char* used = malloc((size_t)n);
@@ -452,7 +456,8 @@ void model_zgeev_batched_opts(int n, int batch, const double* A, double* w, cons
     sweeps[j] = 0;
     work[j] = 0;
     flag[j] = qr(n, a, (zc*)(w + (size_t)j * 2 * n), est ? est + (size_t)j * 2 * n : NULL,
-                 lam ? lam + (size_t)j * 2 * n : NULL, tol, used, &sweeps[j], &work[j], options);
+                 lam ? lam + (size_t)j * 2 * n : NULL, tol, used, &sweeps[j], &work[j], options,
+                 trace ? trace + (size_t)j * trace_cap : NULL, trace_cap);
   }
   free(a);
   free(v);
@@ -461,6 +466,6 @@ void model_zgeev_batched_opts(int n, int batch, const double* A, double* w, cons
 
 void model_zgeev_batched(int n, int batch, const double* A, double* w, const float* est, int* flag, long* sweeps) {
   long long* work = malloc(sizeof(long long) * (size_t)(batch > 0 ? batch : 1));
-  model_zgeev_batched_opts(n, batch, A, w, est, NULL, kUlp, flag, sweeps, work, 0);
+  model_zgeev_batched_opts(n, batch, A, w, est, NULL, kUlp, flag, sweeps, work, 0, NULL, 0);
   free(work);
 }

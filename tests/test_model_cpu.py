@@ -102,3 +102,36 @@ def test_model_gradient_schur_iteration():
     assert 2.8 <= per_eig["wilkinson"] <= 3.6, per_eig
     assert 1.5 <= per_eig["perfect_ulp"] <= 2.0, per_eig
     assert 0.8 <= per_eig["perfect_100ulp"] <= 1.2, per_eig
+
+
+def _lockstep_efficiency(traces, order, width=32):
+    """Matrices sharing a warp run their sweeps in lockstep (one lane each): a sweep costs what
+    the largest active window costs, ~ (m - 1)(m + 2) element-pair updates. Returns the useful
+    fraction of lane time for the given grouping."""
+    def cost(m):
+        return (m - 1) * (m + 2)
+
+    useful = lanes = 0
+    for k in range(0, len(order), width):
+        group = [traces[i] for i in order[k:k + width]]
+        steps = max(len(t) for t in group)
+        useful += sum(int(cost(t).sum()) for t in group)
+        lanes += len(group) * sum(max(int(cost(t[s])) if s < len(t) else 0 for t in group) for s in range(steps))
+    return useful / lanes
+
+
+def test_model_lockstep_divergence_and_grouping():
+    """One matrix per lane (the large-batch shape): window variation between the 32 matrices of
+    a warp wastes only a few percent of lane time, and grouping matrices by the estimator's own
+    sweep count (known before the FP64 QR) does not reduce it."""
+    n, b = 64, 256
+    A = wl.gaussian(b, n, seed=99)
+    est, s32 = lo.model_estimates(A, return_sweeps=True)
+    _, flag, sweeps, work, traces = lo.model_qr_variant(A, est, trace=True)
+    assert (flag == 0).all() and all(len(t) == s for t, s in zip(traces, sweeps))
+    rand = _lockstep_efficiency(traces, np.random.default_rng(0).permutation(b))
+    by_fp32 = _lockstep_efficiency(traces, np.argsort(s32, kind="stable"))
+    by_work = _lockstep_efficiency(traces, np.argsort(work, kind="stable"))
+    assert 0.9 <= rand <= 0.99, rand
+    assert abs(by_fp32 - rand) < 0.01, (rand, by_fp32)
+    assert by_work >= rand, (rand, by_work)
