@@ -87,7 +87,7 @@ def _load():
         lib.model_zgeev_batched.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 5
         lib.model_zgeev_batched_opts.argtypes = ([ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 4
                                                  + [ctypes.c_double] + [ctypes.c_void_p] * 3 + [ctypes.c_int]
-                                                 + [ctypes.c_void_p, ctypes.c_long])
+                                                 + [ctypes.c_void_p, ctypes.c_long, ctypes.c_void_p])
         lib.model_estimates_batched.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                                 ctypes.c_float, ctypes.c_void_p]
         st = lib.cpu_zgeev_open(find_lapack().encode())
@@ -226,13 +226,16 @@ def model_qr(A: np.ndarray, est: np.ndarray | None = None):
 
 def model_qr_variant(A: np.ndarray, est: np.ndarray | None = None, start_row: bool = False,
                      estimate_twice: bool = False, lam: np.ndarray | None = None, tol: float = 2.0 ** -52,
-                     trace: bool = False):
+                     trace: bool = False, scaled: bool = False):
     """model_qr with variants: the two the library does not use (zlahqr's start-row search;
     the estimate as the shift of the second sweep too), and the gradient's Schur iteration
     (``lam``: FP64 eigenvalues as first shifts after each deflation, deflation at ``tol``).
     Returns ``(w, flag, sweeps, work)``, work = element-pair rotation updates per matrix, plus
     with ``trace`` a list of per-matrix arrays: the active window of every sweep (the first
-    16n + 64 sweeps)."""
+    16n + 64 sweeps). ``scaled``: the same iteration with scaled rotations (row and column
+    scale factors, two complex multiply-adds per element pair; n <= 64; not with ``lam``,
+    ``start_row``, ``estimate_twice`` or ``trace``); then a fifth value, the rescales per
+    matrix."""
     lib = _load()
     A = _as_batch(A)
     b, n, _ = A.shape
@@ -244,11 +247,16 @@ def model_qr_variant(A: np.ndarray, est: np.ndarray | None = None, start_row: bo
     lm = None if lam is None else np.ascontiguousarray(lam, dtype=np.complex128).reshape(b, n)
     cap = 16 * n + 64 if trace else 0  # windows beyond 16 sweeps per eigenvalue on average are not kept
     tr = np.zeros((b, cap), np.int32) if trace else None
+    if scaled and (n > 64 or lam is not None or start_row or estimate_twice or trace):
+        raise ValueError("scaled rotations: n <= 64, without lam, start_row, estimate_twice or trace")
+    resc = np.zeros(b, np.int64)
     lib.model_zgeev_batched_opts(n, b, A.ctypes.data, w.ctypes.data, None if e is None else e.ctypes.data,
                                  None if lm is None else lm.ctypes.data, float(tol),
                                  flag.ctypes.data, sweeps.ctypes.data, work.ctypes.data,
-                                 int(start_row) | (2 if estimate_twice else 0),
-                                 None if tr is None else tr.ctypes.data, cap)
+                                 int(start_row) | (2 if estimate_twice else 0) | (4 if scaled else 0),
+                                 None if tr is None else tr.ctypes.data, cap, resc.ctypes.data)
+    if scaled:
+        return w, flag, sweeps, work, resc
     if trace:
         return w, flag, sweeps, work, [tr[j, :sweeps[j]] for j in range(b)]
     return w, flag, sweeps, work

@@ -135,3 +135,25 @@ def test_model_lockstep_divergence_and_grouping():
     assert 0.9 <= rand <= 0.99, rand
     assert abs(by_fp32 - rand) < 0.01, (rand, by_fp32)
     assert by_work >= rand, (rand, by_work)
+
+
+@pytest.mark.parametrize("gen", ["gaussian", "vdv", "companion", "uniform"])
+@pytest.mark.parametrize("n", [2, 8, 33, 64])
+def test_model_scaled_rotations(gen, n):
+    """Scaled rotations (two complex multiply-adds per element pair instead of the plain
+    rotation's 12 FP64 operations): the same sweeps as the plain iteration, LAPACK accuracy,
+    and rescaling of rows/columns only now and then (O(n) each)."""
+    A = wl.GENERATORS[gen](24, n, seed=300 + n)
+    w_ref = lo.zgeev(A, threads=2)[0]
+    fro = np.maximum(np.linalg.norm(A, axis=(1, 2)), 1e-300)
+    _, rc, _ = lo.zgeevx_rconde(A, threads=2)
+    well = (1.0 / np.maximum(rc, 1e-300)).max(axis=1) <= lo.COND_MAX
+    est = lo.model_estimates(A)
+    for hints in (None, est):
+        w0, f0, s0, _ = lo.model_qr_variant(A, hints)
+        w, f, s, work, resc = lo.model_qr_variant(A, hints, scaled=True)
+        assert (f == 0).all() and (f0 == 0).all()
+        assert abs(int(s.sum()) - int(s0.sum())) <= max(2, s0.sum() // 100)
+        err = lo.matched_abs_errors(w, w_ref).max(axis=1) / fro
+        assert np.all(err[well] <= lo.TOL_REL_FRO), err
+        assert resc.sum() <= 8 * s.sum()  # a few row/column rescales per sweep at most
