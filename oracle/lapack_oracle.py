@@ -226,7 +226,7 @@ def model_qr(A: np.ndarray, est: np.ndarray | None = None):
 
 def model_qr_variant(A: np.ndarray, est: np.ndarray | None = None, start_row: bool = False,
                      estimate_twice: bool = False, lam: np.ndarray | None = None, tol: float = 2.0 ** -52,
-                     trace: bool = False, scaled: bool = False):
+                     trace: bool = False, scaled: bool = False, elementary: bool = False):
     """model_qr with variants: the two the library does not use (zlahqr's start-row search;
     the estimate as the shift of the second sweep too), and the gradient's Schur iteration
     (``lam``: FP64 eigenvalues as first shifts after each deflation, deflation at ``tol``).
@@ -235,7 +235,8 @@ def model_qr_variant(A: np.ndarray, est: np.ndarray | None = None, start_row: bo
     16n + 64 sweeps). ``scaled``: the same iteration with scaled rotations (row and column
     scale factors, two complex multiply-adds per element pair; n <= 64; not with ``lam``,
     ``start_row``, ``estimate_twice`` or ``trace``); then a fifth value, the rescales per
-    matrix."""
+    matrix. ``elementary``: Hessenberg form by stabilized elementary similarity transforms
+    (EISPACK comhes) instead of Householder reflectors."""
     lib = _load()
     A = _as_batch(A)
     b, n, _ = A.shape
@@ -253,7 +254,8 @@ def model_qr_variant(A: np.ndarray, est: np.ndarray | None = None, start_row: bo
     lib.model_zgeev_batched_opts(n, b, A.ctypes.data, w.ctypes.data, None if e is None else e.ctypes.data,
                                  None if lm is None else lm.ctypes.data, float(tol),
                                  flag.ctypes.data, sweeps.ctypes.data, work.ctypes.data,
-                                 int(start_row) | (2 if estimate_twice else 0) | (4 if scaled else 0),
+                                 int(start_row) | (2 if estimate_twice else 0) | (4 if scaled else 0)
+                                 | (8 if elementary else 0),
                                  None if tr is None else tr.ctypes.data, cap, resc.ctypes.data)
     if scaled:
         return w, flag, sweeps, work, resc

@@ -86,6 +86,33 @@ static void hessenberg(int n, zc* a, zc* v) {
   }
 }
 
+/* Hessenberg form by stabilized elementary similarity transforms (EISPACK's
+ * comhes: partial pivoting, multipliers of modulus <= 1 by the 1-norm, then
+ * row_i -= m row_{k+1} and col_{k+1} += m col_i): half the multiply-adds of the
+ * Householder reduction, without its unconditional backward stability.
+ * Options bit 3; not used by the library. */
+static void hessenberg_elementary(int n, zc* a) {
+  for (int k = 0; k + 2 < n; ++k) {
+    int p = k + 1;
+    double best = zabs1(H(k + 1, k));
+    for (int i = k + 2; i < n; ++i)
+      if (zabs1(H(i, k)) > best) { best = zabs1(H(i, k)); p = i; }
+    if (best == 0.0) continue;
+    if (p != k + 1) {
+      for (int c = k; c < n; ++c) { zc t = H(p, c); H(p, c) = H(k + 1, c); H(k + 1, c) = t; }
+      for (int r = 0; r < n; ++r) { zc t = H(r, p); H(r, p) = H(r, k + 1); H(r, k + 1) = t; }
+    }
+    zc piv = H(k + 1, k);
+    for (int i = k + 2; i < n; ++i) {
+      zc m = zdiv(H(i, k), piv);
+      if (m.re == 0.0 && m.im == 0.0) continue;
+      H(i, k) = z(0.0, 0.0);
+      for (int c = k + 1; c < n; ++c) H(i, c) = zsub(H(i, c), zmul(m, H(k + 1, c)));
+      for (int r = 0; r < n; ++r) H(r, k + 1) = zadd(H(r, k + 1), zmul(m, H(r, i)));
+    }
+  }
+}
+
 /* Ahues-Tisseur deflation test of subdiagonal entry k of the block [lo, hi],
  * relative to tol (the ulp for eigenvalues; 100 ulp in the gradient's QR). */
 static int negligible(int n, const zc* a, int k, int lo, int hi, double smlnum, double tol) {
@@ -599,7 +626,10 @@ void model_zgeev_batched_opts(int n, int batch, const double* A, double* w, cons
   for (int j = 0; j < batch; ++j) {
     const double* src = A + (size_t)j * 2 * n * n;
     for (size_t e = 0; e < (size_t)n * n; ++e) a[e] = z(src[2 * e], src[2 * e + 1]);
-    hessenberg(n, a, v);
+    if (options & 8)
+      hessenberg_elementary(n, a);
+    else
+      hessenberg(n, a, v);
     sweeps[j] = 0;
     work[j] = 0;
     if (rescales) rescales[j] = 0;

@@ -157,3 +157,20 @@ def test_model_scaled_rotations(gen, n):
         err = lo.matched_abs_errors(w, w_ref).max(axis=1) / fro
         assert np.all(err[well] <= lo.TOL_REL_FRO), err
         assert resc.sum() <= 8 * s.sum()  # a few row/column rescales per sweep at most
+
+
+@pytest.mark.parametrize("gen", ["gaussian", "vdv", "companion", "uniform"])
+def test_model_elementary_hessenberg(gen):
+    """Hessenberg form by stabilized elementary similarity transforms (half the multiply-adds):
+    on these classes as accurate as the Householder reduction (it is not adopted: its
+    stability is not guaranteed in general)."""
+    n = 64
+    A = wl.GENERATORS[gen](24, n, seed=700)
+    w_ref = lo.zgeev(A, threads=2)[0]
+    fro = np.linalg.norm(A, axis=(1, 2))
+    _, rc, _ = lo.zgeevx_rconde(A, threads=2)
+    well = (1.0 / np.maximum(rc, 1e-300)).max(axis=1) <= lo.COND_MAX
+    w, f, _, _ = lo.model_qr_variant(A, elementary=True)
+    assert (f == 0).all()
+    err = lo.matched_abs_errors(w, w_ref).max(axis=1) / fro
+    assert np.all(err[well] <= 1e-13), err
