@@ -114,9 +114,15 @@ class ClockSampler:
             self.proc.wait(timeout=5)
         except subprocess.TimeoutExpired:
             self.proc.kill()
+        return self.summarize(self.lines)
+
+    @staticmethod
+    def summarize(lines: list[str]) -> dict | None:
+        """Median SM clock, max SM clock, max power and the throttle reasons seen as Active in
+        `nvidia-smi --format=csv,noheader,nounits` lines of FIELDS (malformed lines skipped)."""
         sm, smax, power, reasons = [], [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for ln in self.lines:
+        for ln in lines:
             parts = [p.strip() for p in ln.split(",")]
             if len(parts) < 8:
                 continue

@@ -43,3 +43,24 @@ def test_reference_arm_json_line():
     assert d["impl"] == "reference" and d["value"] > 0 and d["higher_is_better"] is True
     assert d["cpu_baseline"]["value"] == d["value"] and d["cpu_baseline"]["cores"] >= 1
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
+
+
+def test_clock_record_summary():
+    """The `clocks` object of the JSON line: median SM clock, max clock and power, and the
+    throttle reasons seen Active during the timed region (nvidia-smi csv, noheader, nounits)."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    lines = [
+        "2070, 2070, 612.5, 0x0000000000000000, Not Active, Not Active, Not Active, Not Active",
+        "2055, 2070, 640.1, 0x0000000000000004, Not Active, Not Active, Not Active, Active",
+        "1980, 2070, 655.0, 0x0000000000000004, Not Active, Not Active, Not Active, Active",
+        "garbage line",
+        "[N/A], 2070, 600.0, 0x0, Not Active, Not Active, Not Active, Not Active",
+    ]
+    s = bench.ClockSampler.summarize(lines)
+    assert s["sm_mhz"] == 2055 and s["sm_max_mhz"] == 2070 and s["samples"] == 3
+    assert s["power_w_max"] == 655.0 and s["reasons"] == ["sw_power_cap"]
+    hot = bench.ClockSampler.summarize(["1500, 2070, 700, 0x8, Not Active, Active, Not Active, Not Active"])
+    assert hot["reasons"] == ["hw_thermal_slowdown"]
+    assert bench.ClockSampler.summarize([]) is None
