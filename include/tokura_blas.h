@@ -25,7 +25,25 @@
 #include <cuda_runtime_api.h>
 #include <cuComplex.h>
 
+/* Public constants and enums of the reference header
+ * (tokura_zgeev_batched_library/include/tokura_blas.h:12-48), same names and
+ * values, so that caller source naming them compiles unchanged. This library
+ * reads none of them: the tuning batch counts describe the reference's
+ * build-time tuner (replaced by tokuraAutotune), and the layout/method enums
+ * name internal stages the reference keeps in its (here opaque) handle. */
 #define TOKURA_ZGEEV_BATCHED_MAX_MATRIX_SIZE 64
+#define TARGET_CUDA_WARP 32
+#define TOKURA_ZGEEV_BATCHED_GEHRD_TUNING_BATCHCOUNT (1024 * 8)
+#define TOKURA_ZGEEV_BATCHED_HSEQR_TUNING_BATCHCOUNT (1024 * 8)
+#define TOKURA_ZGEEV_BATCHED_TUNING_COUNT 1
+
+typedef enum { TOKURA_BLAS_SUCCESS = 0, TOKURA_BLAS_FAIL } TOKURA_ZGEEV_BATCHED_STATUS;
+
+typedef enum { MatrixWise = 0, ElementWise, RowWise, NotSet } TOKURA_ZGEEV_BATCHED_MATRIX_ARRANGEMENT;
+
+typedef enum { ZGEHRD_NORMAL_MWB_METHOD = 0, ZGEHRD_SHARED_MWB_METHOD } TOKURA_ZGEHRD_BATCHED_WHICHFAST;
+
+typedef enum { ZHSEQR_NORMAL_MWB = 0 } TOKURA_ZHSEQR_BATCHED_WHICHFAST;
 
 #if defined(__GNUC__)
 #define TOKURA_API __attribute__((visibility("default")))
@@ -70,6 +88,21 @@ TOKURA_API int tokura_zgeev_batched_gpu(tokurablas_t* handle, int n, int batch_c
                              cudaStream_t cudastream);
 
 #ifdef __cplusplus
+}
+#endif
+
+#ifdef __cplusplus
+#include <stdio.h>
+/* The reference header's error-print helper (tokura_blas.h:152-160): prints
+ * a failed CUDA status with file and line and carries on (it never aborts).
+ * C++ only, as in the reference (default argument). */
+#ifndef gpuErrchk
+#define gpuErrchk(ans) \
+  { gpuAssert((ans), __FILE__, __LINE__); }
+#endif
+inline void gpuAssert(cudaError_t code, const char* file, int line, bool abort = true) {
+  (void)abort;
+  if (code != cudaSuccess) fprintf(stderr, "GPUassert: %s %s %d\n", cudaGetErrorString(code), file, line);
 }
 #endif
 

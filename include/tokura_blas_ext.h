@@ -274,13 +274,17 @@ TOKURA_API int tokuraSetRealConfig(tokurablas_t* handle, int n, int lanes_per_ma
  * (held by every GPU that loads it until exit), so 16*n*n*batch_count must be
  * <= tokura_zgeev_noalloc_max_bytes(): at most 512 matrices of order 64,
  * 2048 of order 32 (the shift hints of tokuraSetShiftHints are used when
- * their 8*n*batch_count bytes also fit). The first call on a device looks up that array's device
- * address, so make it before any stream capture starts. All calls share the
+ * their (8*n + 4)*batch_count bytes of estimates and phase state also fit:
+ * up to 508 matrices of order 64, 2016 of order 32). The first call on a
+ * device looks up that array's device address, so make it before any stream
+ * capture starts; the address is kept for the life of the process, so calls
+ * after a cudaDeviceReset of that device are not supported. The handle's
+ * device must be the current device (else 1). All calls share the
  * array: calls that overlap on the GPU race and must be ordered by the
  * caller (e.g. one stream). A is not modified.
  * Returns the codes of tokura_zgeev_batched_gpu (no -5: there is no work),
- * -8 if the batch exceeds the static array, 1 if the address lookup or the
- * launch fails. */
+ * -8 if the batch exceeds the static array, 1 if the current device is not
+ * the handle's or the address lookup or the launch fails. */
 TOKURA_API int tokura_zgeev_batched_gpu_noalloc(tokurablas_t* handle, int n, int batch_count, cuDoubleComplex* A,
                                                 cuDoubleComplex* eigenvalues, char* flag, cudaStream_t cudastream);
 

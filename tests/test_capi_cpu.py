@@ -179,6 +179,51 @@ def test_c_caller_compiles_against_header(tmp_path):
     assert r.returncode == 0, r.stderr
 
 
+def test_reference_header_constants_and_enums(tmp_path):
+    """The reference header's public macros and enums (tokura_blas.h:12-48 of the reference)
+    exist with the same names and values, in C and in C++."""
+    body = ("#include \"tokura_blas.h\"\n"
+            "typedef char a1[TARGET_CUDA_WARP == 32 ? 1 : -1];\n"
+            "typedef char a2[TOKURA_ZGEEV_BATCHED_MAX_MATRIX_SIZE == 64 ? 1 : -1];\n"
+            "typedef char a3[TOKURA_ZGEEV_BATCHED_GEHRD_TUNING_BATCHCOUNT == 8192 ? 1 : -1];\n"
+            "typedef char a4[TOKURA_ZGEEV_BATCHED_HSEQR_TUNING_BATCHCOUNT == 8192 ? 1 : -1];\n"
+            "typedef char a5[TOKURA_ZGEEV_BATCHED_TUNING_COUNT == 1 ? 1 : -1];\n"
+            "typedef char a6[TOKURA_BLAS_SUCCESS == 0 && TOKURA_BLAS_FAIL == 1 ? 1 : -1];\n"
+            "typedef char a7[MatrixWise == 0 && ElementWise == 1 && RowWise == 2 && NotSet == 3 ? 1 : -1];\n"
+            "typedef char a8[ZGEHRD_NORMAL_MWB_METHOD == 0 && ZGEHRD_SHARED_MWB_METHOD == 1 ? 1 : -1];\n"
+            "typedef char a9[ZHSEQR_NORMAL_MWB == 0 ? 1 : -1];\n"
+            "TOKURA_ZGEEV_BATCHED_STATUS s = TOKURA_BLAS_FAIL;\n"
+            "TOKURA_ZGEEV_BATCHED_MATRIX_ARRANGEMENT m = NotSet;\n"
+            "TOKURA_ZGEHRD_BATCHED_WHICHFAST g = ZGEHRD_SHARED_MWB_METHOD;\n"
+            "TOKURA_ZHSEQR_BATCHED_WHICHFAST q = ZHSEQR_NORMAL_MWB;\n")
+    for compiler, ext, extra in (("gcc", "c", ["-std=c99"]), ("g++", "cpp", ["-std=c++17"])):
+        src = tmp_path / f"consts.{ext}"
+        cpp_tail = "void f(void) { gpuErrchk(cudaSuccess); }\n" if ext == "cpp" else ""
+        src.write_text(body + cpp_tail)
+        r = subprocess.run([compiler] + extra + ["-Wall", "-Werror", "-Wno-unused-variable", "-c", str(src),
+                            "-I", os.path.join(ROOT, "include"), "-I", "/usr/local/cuda/include",
+                            "-o", str(tmp_path / f"consts_{ext}.o")], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+
+
+REFERENCE_DRIVER = "/root/reference/stream_test/main.cu"
+
+
+@pytest.mark.skipif(not os.path.exists(REFERENCE_DRIVER), reason="the reference's sources are not mounted here")
+def test_reference_driver_compiles_against_header(tmp_path):
+    """The reference's own MKL-free throughput driver (stream_test/main.cu, compiled there by
+    stream_test/compile.sh:1 against the reference's include/) compiles unchanged against this
+    library's include/ (compile only: nothing of the reference is linked or run)."""
+    r = subprocess.run(["nvcc", "-c", REFERENCE_DRIVER, "-I", os.path.join(ROOT, "include"), "-Xcompiler",
+                        "-fopenmp", "-gencode", "arch=compute_103a,code=sm_103a", "-o", str(tmp_path / "driver.o")],
+                       capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    nm = subprocess.run(["nm", "-u", str(tmp_path / "driver.o")], capture_output=True, text=True).stdout
+    # C linkage here: the driver's object refers to the plain names this library exports.
+    for sym in ("tokuraCreate", "tokura_get_zgeeveigenvaluesgetworspacesize", "tokura_zgeev_batched_gpu"):
+        assert sym in nm.split(), sym
+
+
 def test_ragged_workspace_size(lib):
     ws = api.tokura_get_zgeev_ragged_workspacesize
     size_max = 2 ** 64 - 1

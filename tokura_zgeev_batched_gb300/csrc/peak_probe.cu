@@ -3,9 +3,9 @@
 // The path is bound by the FP64 CUDA-core rate (no step is a dense
 // contraction), which the device's published figures do not pin down for a
 // given clock. This kernel measures it: every thread runs 8 independent
-// dependent-FMA chains, one 128-thread block per SM-resident slot, so the
-// FP64 pipe of every SM sub-partition is saturated. Reported as FP64 FLOP/s
-// (2 flops per FMA).
+// dependent-FMA chains in 256-thread blocks, two blocks per SM (16 warps per
+// SM, 4 per sub-partition), so the FP64 pipe of every SM sub-partition is
+// saturated. Reported as FP64 FLOP/s (2 flops per FMA).
 #include <cuda_runtime.h>
 
 #include "../../include/tokura_blas_ext.h"

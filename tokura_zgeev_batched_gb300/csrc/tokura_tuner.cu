@@ -4,7 +4,7 @@
 // TUNING_main.cu:89-227, which timed threads-per-matrix for each n once on
 // 8192 random matrices and wrote #define tables that were compiled into the
 // library, include/tokura_zhseqr_parameters.h). Here the candidates — lanes
-// per matrix (1, 2, 4) x threads per block (64, 128, 256) — are timed with
+// per matrix (1, 2, 4, 8) x threads per block (32, 64, 128, 256) — are timed with
 // CUDA events on seeded synthetic complex Gaussian matrices at the caller's
 // batch size, the fastest shape is stored in the handle, and the table can be
 // saved to / loaded from a text file keyed by device name and SM count.

@@ -18,7 +18,9 @@
 // Host code must not hand the array's name to a kernel: on the host it is only
 // a stand-in symbol. The device address is obtained once per device, with that
 // device current, by cudaGetSymbolAddress on the first call made on that device
-// (so make that first call before any stream capture begins). All calls share
+// (so make that first call before any stream capture begins); the address is
+// cached for the life of the process, so a cudaDeviceReset of that device
+// invalidates it and later calls are unsupported. All calls share
 // the array and it keeps the previous call's contents; the kernel overwrites
 // every staging element before reading it, so nothing needs clearing. Calls
 // whose executions overlap on the GPU (different streams, or different host
@@ -77,6 +79,10 @@ extern "C" TOKURA_API int tokura_zgeev_batched_gpu_noalloc(tokurablas_t* handle,
   const bool hints = tzg::use_shift_hints(handle, n) &&
                      need + (sizeof(float2) * (size_t)n + sizeof(int)) * (size_t)batch_count <=
                          tzg::kNoAllocScratchBytes;
+  // The estimator runs on the handle's second stream, which belongs to the
+  // handle's device: the scratch array must be that device's too.
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev != handle->device) return 1;
   double2* scratch = nullptr;
   if (tzg::noalloc_scratch_ptr(&scratch) != cudaSuccess) return 1;
   const tzg::PlainConfig cfg = tzg::plain_config_for(handle, n, batch_count);
