@@ -238,19 +238,32 @@ def phase(name: str) -> None:
     print(f"[bench {time.strftime('%H:%M:%S')}] {name}", file=sys.stderr, flush=True)
 
 
-def spot_check(A, eig, flag, count: int) -> dict:
-    """Max/p99 of max|dlambda|/||A||_F against LAPACK zgeev on an evenly spaced sample of the batch."""
-    import torch
+# Parity at configuration scale: LAPACK zgeev on every matrix of a batch for flag parity
+# (CHECK_FULL_FLAGS) and the matched eigenvalue error, with zgeevx condition numbers, on a
+# seeded random subset of CHECK_SUBSET matrices (the whole batch when it is smaller).
+CHECK_SUBSET = 10000
+CHECK_FULL_FLAGS = True
 
+
+def _parity_fields(rep: dict, seconds: float) -> dict:
+    return {"checked": rep["checked"], "flags_checked": rep["flags_checked"],
+            "max_rel_err_fro": rep["max_rel_err"], "p99_rel_err_fro": rep["p99_rel_err"],
+            "flag_mismatch": rep["flag_mismatch"], "lapack_fail": rep["lapack_fail"],
+            "gpu_flagged": rep["gpu_flagged"], "cond_le_1e3": rep.get("well_conditioned"),
+            "max_rel_err_fro_cond_le_1e3": rep.get("max_rel_err_well"),
+            "p99_rel_err_fro_cond_le_1e3": rep.get("p99_rel_err_well"), "cpu_seconds": seconds}
+
+
+def scale_check(A, eig, flag, seed: int, subset: int | None = None, full_flags: bool | None = None) -> dict:
+    """Parity of a whole uniform batch against LAPACK zgeev (flags of every matrix, matched
+    errors on a seeded subset); max/p99 of max|dlambda|/||A||_F."""
     from oracle import lapack_oracle as lo
 
-    batch = A.shape[0]
-    idx = torch.arange(0, batch, max(1, batch // count), device=A.device)[:count]
-    rep = lo.parity_report(A[idx].cpu().numpy(), eig[idx].cpu().numpy(), flag[idx].cpu().numpy())
-    return {"checked": int(idx.numel()), "max_rel_err_fro": rep["max_rel_err"], "p99_rel_err_fro": rep["p99_rel_err"],
-            "flag_mismatch": rep["flag_mismatch"], "lapack_fail": rep["lapack_fail"],
-            "cond_le_1e3": rep.get("well_conditioned"), "max_rel_err_fro_cond_le_1e3": rep.get("max_rel_err_well"),
-            "p99_rel_err_fro_cond_le_1e3": rep.get("p99_rel_err_well")}
+    t0 = time.perf_counter()
+    rep = lo.batch_parity(A.cpu().numpy(), eig.cpu().numpy(), flag.cpu().numpy(),
+                          subset=CHECK_SUBSET if subset is None else subset, seed=seed,
+                          full_flags=CHECK_FULL_FLAGS if full_flags is None else full_flags)
+    return _parity_fields(rep, time.perf_counter() - t0)
 
 
 def time_ms(fn, reps: int, stream) -> float:
@@ -284,7 +297,7 @@ def measure_config1(h, dev, stream, peak, call) -> dict:
     rate = batch / (ms * 1e-3)
     out = {"n": n, "batch": batch, "ms": ms, "matrices_per_s": rate, "fp64_frac": flops_per_matrix(n) * rate / peak,
            "lanes_per_matrix": h.plain_config(n, batch)[0], "flagged": int((flag != 0).sum().item()),
-           "parity": spot_check(A, eig, flag, 256)}
+           "parity": scale_check(A, eig, flag, seed=SEED + 1, subset=batch)}
     # The same call on a handle tuned for this order and batch (tokuraAutotune).
     ht = api.Handle()
     if ht.autotune(n, n, batch, stream.cuda_stream) == 0:
@@ -427,6 +440,7 @@ def measure_config4(h, dev, stream, peak, batch: int = 50000, orders=(16, 48)) -
                                                 flag.data_ptr(), s) == 0
 
         fwd()
+        fwd_parity = scale_check(A, eig, flag, seed=SEED + 40 + n)
         gbar = (torch.exp(eig.real) + 2 * eig).contiguous()
 
         def bwd():
@@ -453,6 +467,7 @@ def measure_config4(h, dev, stream, peak, batch: int = 50000, orders=(16, 48)) -
             "fp64_frac_fwd_bwd": (f_fwd + f_bwd) * batch / ((ms_f + ms_b) * 1e-3) / peak,
             "grad_rel_err_vs_torch_cpu_16": rel,
             "flagged_forward": int((flag != 0).sum().item()), "flagged_backward": int((bflag != 0).sum().item()),
+            "forward_parity": fwd_parity,
         }
         del A, eig, flag, work, gA, bflag, bwork, gbar
         torch.cuda.empty_cache()
@@ -605,22 +620,14 @@ def measure_ragged(h, dev, stream, peak, batch: int = 200000) -> dict:
 
     ms_ragged = time_ms(ragged_call, 3, stream)
     flagged = int((flag != 0).sum().item())
-    # parity sample: 4 matrices of each order, compared with LAPACK
+    # Parity at full scale: LAPACK on every matrix (flags), matched errors on a seeded subset.
     from oracle import lapack_oracle as lo
 
     eoffs = np.concatenate([[0], np.cumsum(ns.astype(np.int64))[:-1]])
-    eig_h = eig.cpu().numpy()
-    flag_h = flag.cpu().numpy()
-    worst, rels = 0.0, []
-    for k in range(1, 65):
-        js = np.where(ns == k)[0][:4]
-        if len(js) == 0:
-            continue
-        mats = np.stack([A[offsets[j]:offsets[j] + k * k].cpu().numpy().reshape(k, k) for j in js])
-        w = np.stack([eig_h[eoffs[j]:eoffs[j] + k] for j in js])
-        rep = lo.parity_report(mats, w, flag_h[js], with_cond=False)
-        rels.extend(list(rep["rel_err"][np.isfinite(rep["rel_err"])]))
-    parity = {"checked": len(rels), "max_rel_err_fro": float(np.max(rels)), "p99_rel_err_fro": float(np.percentile(rels, 99))}
+    t_chk = time.perf_counter()
+    rep = lo.ragged_batch_parity(A.cpu().numpy(), ns, offsets, eig.cpu().numpy(), eoffs, flag.cpu().numpy(),
+                                 subset=CHECK_SUBSET, seed=SEED + 3, full_flags=CHECK_FULL_FLAGS)
+    parity = _parity_fields(rep, time.perf_counter() - t_chk)
     # CUDA graph of the ragged call (planning kernels + persistent solver).
     graph_ms = None
     try:
@@ -751,7 +758,7 @@ def run_ours(args):
     # Parity spot check of the timed output against LAPACK (rank 0, outside timing).
     parity = None
     if rank == 0 and not args.no_check:
-        parity = spot_check(A, eig, flag, 256)
+        parity = scale_check(A, eig, flag, seed=SEED)
 
     kern_avg = statistics.mean(kern_ms)
     achieved = flops_per_matrix(N) * BATCH / (kern_avg * 1e-3)
@@ -882,7 +889,7 @@ def run_ours(args):
                                "fp64_frac": flops_per_matrix(n) * rate / peak,
                                "flagged": int((flag != 0).sum().item())}
                 if rank == 0 and not args.no_check:
-                    res[str(n)]["parity"] = spot_check(A, eig, flag, 128)
+                    res[str(n)]["parity"] = scale_check(A, eig, flag, seed=SEED + 17 * n)
                 del A, eig, flag, work
                 torch.cuda.empty_cache()
             sweep[cls] = res
@@ -930,7 +937,7 @@ def run_ours(args):
                        "shift_hints": "FP32 estimator on a second stream beside the FP64 Hessenberg kernel, then "
                                       "the FP64 QR kernel" if N >= SHIFT_HINT_MIN_N else "off (n < 12)"},
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "clocks": clocks,
-            "gpu_launches": args.steps * (3 if N >= SHIFT_HINT_MIN_N else 1), "flagged": flagged, "parity_spot_check": parity, "sweep": sweep,
+            "gpu_launches": args.steps * (3 if N >= SHIFT_HINT_MIN_N else 1), "flagged": flagged, "parity": parity, "sweep": sweep,
             "config1_n32_10000": config1, "ragged": ragged, "config4_backward": config4,
             "config5_ragged_gd_graph": config5, "real_dgeev_n64": real, "eigenvectors_n64": vectors,
         }
@@ -988,8 +995,15 @@ def main():
                     help="run one configuration alone (profiling cases); --batch sets its size")
     ap.add_argument("--n", type=int, default=N, help="matrix order of the timed workload (profiling cases)")
     ap.add_argument("--batch", type=int, default=0, help="matrices per GPU (default: 4 GiB of input)")
+    ap.add_argument("--check-subset", type=int, default=CHECK_SUBSET,
+                    help="matrices per configuration whose eigenvalues are matched against LAPACK")
+    ap.add_argument("--check-flags", choices=["all", "subset"], default="all",
+                    help="LAPACK on every matrix of each batch for flag parity, or on the subset only")
     args = ap.parse_args()
     set_workload(args.n, args.batch)
+    global CHECK_SUBSET, CHECK_FULL_FLAGS
+    CHECK_SUBSET = args.check_subset
+    CHECK_FULL_FLAGS = args.check_flags == "all"
     if args.impl == "reference":
         run_reference(args)
     elif args.only is not None:

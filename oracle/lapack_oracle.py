@@ -277,39 +277,61 @@ def model_estimates(A: np.ndarray, tol: float = 1e-5, return_sweeps: bool = Fals
     return (est, sweeps) if return_sweeps else est
 
 
-def matched_abs_errors(w_test: np.ndarray, w_ref: np.ndarray) -> np.ndarray:
-    """Per-eigenvalue |error| after optimal per-matrix matching; shape [batch, n], in w_ref's order."""
+def _match_one(a: np.ndarray, b: np.ndarray) -> np.ndarray:
+    """Per-eigenvalue |error| of one matrix (w_ref a, w_test b) after an optimal assignment."""
     from scipy.optimize import linear_sum_assignment
 
-    w_test = np.atleast_2d(w_test)
-    w_ref = np.atleast_2d(w_ref)
-    out = np.empty(w_ref.shape, np.float64)
-    for k in range(w_ref.shape[0]):
-        a, b = w_ref[k], w_test[k]
-        d = np.abs(a[:, None] - b[None, :])
-        if not np.all(np.isfinite(d)):
-            out[k] = np.inf
-            continue
-        # Fast path: nearest neighbours already form a permutation.
-        nn = np.argmin(d, axis=1)
-        if len(np.unique(nn)) == len(nn):
-            out[k] = d[np.arange(len(a)), nn]
-            # nearest-neighbour assignment is optimal for the max metric only if no
-            # other permutation lowers the maximum; verify with the Hungarian method
-            # when the errors are not tiny compared to the gaps.
-            gaps = np.sort(d, axis=1)
-            if gaps.shape[1] < 2 or np.all(out[k] * 4 < gaps[:, 1]):
-                continue
-        r, c = linear_sum_assignment(d)
-        out[k][r] = d[r, c]
+    d = np.abs(a[:, None] - b[None, :])
+    if not np.all(np.isfinite(d)):
+        return np.full(a.shape, np.inf)
+    out = np.empty(a.shape, np.float64)
+    r, c = linear_sum_assignment(d)
+    out[r] = d[r, c]
+    return out
+
+
+def matched_abs_errors(w_test: np.ndarray, w_ref: np.ndarray, block: int = 1024) -> np.ndarray:
+    """Per-eigenvalue |error| after optimal per-matrix matching; shape [batch, n], in w_ref's order.
+
+    Vectorized over blocks of matrices: where every reference eigenvalue's nearest test
+    eigenvalue is distinct (a permutation) and each such error is below a quarter of the
+    distance to the second-nearest one, that permutation is the optimal assignment and is
+    taken as is; any other matrix (or one with non-finite values) goes through the
+    Hungarian method (scipy's linear_sum_assignment), matrix by matrix."""
+    w_test = np.atleast_2d(np.asarray(w_test))
+    w_ref = np.atleast_2d(np.asarray(w_ref))
+    b, n = w_ref.shape
+    out = np.empty((b, n), np.float64)
+    for s0 in range(0, b, block):
+        a = w_ref[s0:s0 + block]
+        t = w_test[s0:s0 + block]
+        m = a.shape[0]
+        with np.errstate(invalid="ignore"):
+            d = np.abs(a[:, :, None] - t[:, None, :])  # [m, n(ref), n(test)]
+        fin = np.isfinite(d).all(axis=(1, 2))
+        d = np.where(np.isfinite(d), d, np.inf)
+        nn = np.argmin(d, axis=2)
+        best = np.take_along_axis(d, nn[:, :, None], axis=2)[:, :, 0]
+        if n > 1:
+            perm = (np.diff(np.sort(nn, axis=1), axis=1) != 0).all(axis=1)
+            second = np.partition(d, 1, axis=2)[:, :, 1]
+            gap = (best * 4 < second).all(axis=1)
+            good = fin & perm & gap
+        else:
+            good = fin
+        out[s0:s0 + m][good] = best[good]
+        for k in np.nonzero(~good)[0]:
+            out[s0 + k] = _match_one(a[k], t[k]) if fin[k] else np.inf
     return out
 
 
 def parity_report(A: np.ndarray, w_test: np.ndarray, flag_test: np.ndarray, threads: int | None = None,
-                  with_cond: bool = True) -> dict:
-    """Compares eigenvalues/flags against LAPACK zgeev on the same inputs."""
+                  with_cond: bool = True, w_ref: np.ndarray | None = None, info: np.ndarray | None = None) -> dict:
+    """Compares eigenvalues/flags against LAPACK zgeev on the same inputs (``w_ref``/``info``:
+    LAPACK's results when already computed for these matrices)."""
     A = _as_batch(A)
-    w_ref, info, _ = zgeev(A, threads)
+    if w_ref is None or info is None:
+        w_ref, info, _ = zgeev(A, threads)
     fro = np.sqrt(np.sum(np.abs(A) ** 2, axis=(1, 2)))
     fro = np.where(fro == 0, 1.0, fro)
     ok = (info == 0) & (np.asarray(flag_test) == 0)
@@ -333,8 +355,96 @@ def parity_report(A: np.ndarray, w_test: np.ndarray, flag_test: np.ndarray, thre
         rep["well_conditioned"] = int(well.sum())
         rep["max_rel_err_well"] = float(np.nanmax(rel[well])) if well.any() else float("nan")
         rep["p99_rel_err_well"] = float(np.nanpercentile(rel[well], 99)) if well.any() else float("nan")
+        rep["well"] = well
     rep["rel_err"] = rel
     return rep
+
+
+def batch_parity(A: np.ndarray, w_test: np.ndarray, flag_test: np.ndarray, subset: int = 10000, seed: int = 0,
+                 full_flags: bool = True, threads: int | None = None) -> dict:
+    """Parity of a whole batch at its full size: LAPACK zgeev on every matrix for flag parity
+    (``full_flags``; else on the subset only), and the matched eigenvalue error, with zgeevx
+    condition numbers, on a seeded random subset of ``subset`` matrices (all of them when the
+    batch is no larger). Returns the report of :func:`parity_report` on the subset (without
+    ``rel_err``) plus ``flags_checked``, ``flag_mismatch`` / ``lapack_fail`` over those,
+    ``gpu_flagged`` and ``checked``."""
+    A = _as_batch(A)
+    b = A.shape[0]
+    flag_test = np.asarray(flag_test).reshape(b)
+    w_test = np.asarray(w_test).reshape(b, -1)
+    if b <= subset:
+        pick = np.arange(b)
+    else:
+        pick = np.sort(np.random.default_rng(seed).choice(b, size=subset, replace=False))
+    if full_flags:
+        w_all, info_all, _ = zgeev(A, threads)
+        w_ref, info = w_all[pick], info_all[pick]
+        flags_checked = b
+        mism = int(np.sum((info_all != 0) != (flag_test != 0)))
+        fail = int(np.sum(info_all != 0))
+    else:
+        w_ref, info, _ = zgeev(A[pick], threads)
+        flags_checked = len(pick)
+        mism = int(np.sum((info != 0) != (flag_test[pick] != 0)))
+        fail = int(np.sum(info != 0))
+    rep = parity_report(A[pick], w_test[pick], flag_test[pick], threads, True, w_ref=w_ref, info=info)
+    rep.pop("rel_err")
+    rep.pop("well")
+    rep.update({"checked": int(len(pick)), "flags_checked": int(flags_checked), "flag_mismatch": mism,
+                "lapack_fail": fail, "gpu_flagged": int(np.count_nonzero(flag_test))})
+    return rep
+
+
+def ragged_batch_parity(A_flat: np.ndarray, ns: np.ndarray, offsets: np.ndarray, w_flat: np.ndarray,
+                        eig_offsets: np.ndarray, flag_test: np.ndarray, subset: int = 10000, seed: int = 0,
+                        full_flags: bool = True, threads: int | None = None) -> dict:
+    """:func:`batch_parity` for a ragged batch: matrix j has order ``ns[j]`` and its column-major
+    entries start at ``A_flat[offsets[j]]``; its eigenvalues at ``w_flat[eig_offsets[j]]``.
+    LAPACK runs per order on every matrix (``full_flags``) or on the seeded subset only; the
+    matched error (with zgeevx condition numbers) covers the subset."""
+    A_flat = np.asarray(A_flat).reshape(-1)
+    ns = np.asarray(ns).astype(np.int64)
+    offsets = np.asarray(offsets).astype(np.int64)
+    eig_offsets = np.asarray(eig_offsets).astype(np.int64)
+    flag_test = np.asarray(flag_test).reshape(-1)
+    w_flat = np.asarray(w_flat).reshape(-1)
+    b = ns.shape[0]
+    in_sub = np.zeros(b, bool)
+    if b <= subset:
+        in_sub[:] = True
+    else:
+        in_sub[np.random.default_rng(seed).choice(b, size=subset, replace=False)] = True
+    mism = fail = flags_checked = 0
+    rels, wells = [], []
+    for k in np.unique(ns):
+        js = np.nonzero(ns == k)[0]
+        sel = js if full_flags else js[in_sub[js]]
+        if sel.size == 0:
+            continue
+        k = int(k)
+        mats = A_flat[offsets[sel][:, None] + np.arange(k * k)[None, :]].reshape(sel.size, k, k)
+        w_ref, info, _ = zgeev(mats, threads)
+        f = flag_test[sel]
+        mism += int(np.sum((info != 0) != (f != 0)))
+        fail += int(np.sum(info != 0))
+        flags_checked += int(sel.size)
+        sub = in_sub[sel]
+        if not sub.any():
+            continue
+        wt = w_flat[eig_offsets[sel[sub]][:, None] + np.arange(k)[None, :]]
+        rep = parity_report(mats[sub], wt, f[sub], threads, True, w_ref=w_ref[sub], info=info[sub])
+        rels.append(rep["rel_err"])
+        wells.append(rep["well"])
+    rel = np.concatenate(rels)
+    well = np.concatenate(wells)
+    ok = np.isfinite(rel)
+    return {"batch": int(b), "checked": int(in_sub.sum()), "flags_checked": flags_checked, "flag_mismatch": mism,
+            "lapack_fail": fail, "gpu_flagged": int(np.count_nonzero(flag_test)),
+            "max_rel_err": float(np.nanmax(rel)) if ok.any() else float("nan"),
+            "p99_rel_err": float(np.nanpercentile(rel[ok], 99)) if ok.any() else float("nan"),
+            "well_conditioned": int(well.sum()),
+            "max_rel_err_well": float(np.nanmax(rel[well])) if well.any() else float("nan"),
+            "p99_rel_err_well": float(np.nanpercentile(rel[well], 99)) if well.any() else float("nan")}
 
 
 def real_parity_report(A: np.ndarray, wr: np.ndarray, wi: np.ndarray, flag_test: np.ndarray,
