@@ -53,6 +53,17 @@ def flops_per_matrix(n: int) -> float:
     return 40.0 * n ** 3
 
 
+# Real FP64 flops of the backward per matrix, in units of n^3 (FMA = 2 flops), counted from
+# its steps (tokura_zgeev_batched_gb300/csrc/zgeev_backward.cuh) at leading order:
+#   Householder Hessenberg keeping tau        16 * sum_m m (m + n)        = 40/3
+#   Q from the reflectors                     16 * sum_m m^2              = 16/3
+#   Schur QR, full-width updates, Q rotated   20 flops per element pair, ~2n pairs per rotation,
+#     one sweep per eigenvalue (perfect shifts; CPU model ~1.0)  20 * 2n * n^2/2 = 20
+#   X and Y by back-substitution              8 * 2 * sum_k k^2/2         = 8/3
+#   M = Y Z, P = Q M, Abar = P Q^H            8 * (n^3/6 + n^3/2 + n^3)   = 40/3
+BWD_FLOPS_PER_N3 = 40.0 / 3 + 16.0 / 3 + 20.0 + 8.0 / 3 + 40.0 / 3
+
+
 def bytes_per_matrix(n: int) -> int:
     return 16 * n * n + 16 * n + 1
 
@@ -458,20 +469,22 @@ def measure_config4(h, dev, stream, peak, batch: int = 50000, orders=(16, 48)) -
         got = gA[idx].cpu().numpy()
         rel = float(np.max(np.linalg.norm(got - ref, axis=(1, 2)) / np.linalg.norm(ref, axis=(1, 2))))
         f_fwd = 40.0 * n ** 3
-        f_bwd = 132.0 * n ** 3
+        f_bwd = BWD_FLOPS_PER_N3 * n ** 3
         out[str(n)] = {
             "batch": batch, "ms_forward": ms_f, "ms_backward": ms_b,
             "matrices_per_s_forward": batch / (ms_f * 1e-3),
             "matrices_per_s_fwd_bwd": batch / ((ms_f + ms_b) * 1e-3),
             "fwd_bwd_over_fwd": (ms_f + ms_b) / ms_f,
             "fp64_frac_fwd_bwd": (f_fwd + f_bwd) * batch / ((ms_f + ms_b) * 1e-3) / peak,
+            "fp64_frac_backward": f_bwd * batch / (ms_b * 1e-3) / peak,
             "grad_rel_err_vs_torch_cpu_16": rel,
             "flagged_forward": int((flag != 0).sum().item()), "flagged_backward": int((bflag != 0).sum().item()),
             "forward_parity": fwd_parity,
         }
         del A, eig, flag, work, gA, bflag, bwork, gbar
         torch.cuda.empty_cache()
-    out["convention"] = "F_fwd = 40 n^3, F_bwd = 132 n^3 flop per matrix"
+    out["convention"] = (f"F_fwd = 40 n^3, F_bwd = {BWD_FLOPS_PER_N3:.2f} n^3 flop per matrix (the backward's "
+                         f"operation count with one perfect-shift sweep per eigenvalue)")
     return out
 
 
@@ -543,9 +556,18 @@ def measure_config5(h, dev, stream, peak, batch: int = 20000, steps: int = 100) 
             A.sub_(lr * g)
         return loss
 
+    def per_matrix(lam):
+        """Per matrix: max Re lambda and the smoothed abscissa tau*logsumexp(Re lambda / tau)."""
+        x = lam.real / tau
+        m = torch.full((batch,), -float("inf"), dtype=torch.float64, device=dev).scatter_reduce(
+            0, seg, x, reduce="amax")
+        ssum = torch.zeros(batch, dtype=torch.float64, device=dev).index_add(0, seg, torch.exp(x - m[seg]))
+        return m * tau, tau * (torch.log(ssum) + m)
+
     with torch.no_grad():
-        before = class_max(api.zgeev_ragged(A.detach(), n_d, offsets=o_d, handle=h, work=work_f,
-                                            total_eigenvalues=total_eig)[0])
+        lam0 = api.zgeev_ragged(A.detach(), n_d, offsets=o_d, handle=h, work=work_f, total_eigenvalues=total_eig)[0]
+        before = class_max(lam0)
+        maxre0, abscissa0 = per_matrix(lam0)
     side = torch.cuda.Stream(dev)
     side.wait_stream(stream)
     with torch.cuda.stream(side):
@@ -571,14 +593,63 @@ def measure_config5(h, dev, stream, peak, batch: int = 20000, steps: int = 100) 
         lam_final, flag = api.zgeev_ragged(A.detach(), n_d, offsets=o_d, handle=h, work=work_f,
                                            total_eigenvalues=total_eig)
         after = class_max(lam_final)
+        maxre1, abscissa1 = per_matrix(lam_final)
     ms_fwd = time_ms(lambda: api.zgeev_ragged(A.detach(), n_d, offsets=o_d, handle=h, work=work_f,
                                               total_eigenvalues=total_eig), 3, stream)
     del graph
+    diagnosis = guarded(lambda: diagnose_config5(A0, A.detach(), ns, offsets, maxre0, maxre1, tau, lr, steps))
+    rose = (maxre1 > maxre0)
+    rose_by_class = {}
+    for lo_, hi_ in ((8, 16), (16, 32), (32, 48), (48, 65)):
+        sel = (n_d >= lo_) & (n_d < hi_)
+        rose_by_class[f"{lo_}-{min(hi_, 64)}"] = {"matrices": int(sel.sum().item()),
+                                                   "max_re_lambda_rose": int((rose & sel).sum().item())}
     return {"batch": batch, "steps": steps, "ms_total": ms, "ms_per_step": ms / steps,
             "matrices_per_s_fwd_bwd": batch * steps / (ms * 1e-3), "ms_forward_only": ms_fwd,
             "fwd_bwd_over_fwd": (ms / steps) / ms_fwd, "max_re_lambda_before": before,
-            "max_re_lambda_after": after, "final_loss": final_loss,
-            "flagged_after": int((flag != 0).sum().item())}
+            "max_re_lambda_after": after, "initial_loss": float(abscissa0.sum().item()),
+            "loss_after_last_step": float(abscissa1.sum().item()),
+            "loss_at_last_step_start": final_loss, "rose_by_class": rose_by_class,
+            "diagnosis": diagnosis, "flagged_after": int((flag != 0).sum().item())}
+
+
+def diagnose_config5(A0, A1, ns, offsets, maxre0, maxre1, tau, lr, steps, worst: int = 10) -> dict:
+    """The matrices whose max Re lambda rose most over the GD run: their largest eigenvalue
+    condition number (LAPACK zgeevx on the initial matrix) and the same run of `steps` GD steps
+    repeated on the CPU with torch.linalg.eigvals (FP64) and autograd, per matrix (the loss is
+    a sum over matrices, so each matrix's trajectory is independent)."""
+    import numpy as np
+    import torch
+
+    from oracle import lapack_oracle as lo
+
+    rise = (maxre1 - maxre0).cpu().numpy()
+    idx = np.argsort(-rise)[:worst]
+    out = []
+    for j in idx:
+        k = int(ns[j])
+        o = int(offsets[j])
+        M0 = A0[o:o + k * k].cpu().numpy().reshape(k, k)  # the column-major buffer read row-major: A^T
+        _, rc, _ = lo.zgeevx_rconde(M0[None])
+        X = torch.from_numpy(M0.copy()).requires_grad_(True)
+        for _ in range(steps):
+            lam = torch.linalg.eigvals(X)
+            loss = tau * torch.logsumexp(lam.real / tau, 0)
+            (g,) = torch.autograd.grad(loss, X)
+            with torch.no_grad():
+                X -= lr * g
+        with torch.no_grad():
+            cpu_final = float(torch.linalg.eigvals(X).real.max())
+        gpu_final_A = A1[o:o + k * k].cpu().numpy().reshape(k, k)
+        out.append({"n": k, "max_re_lambda_before": float(maxre0[j]), "max_re_lambda_after_gpu": float(maxre1[j]),
+                    "max_re_lambda_after_cpu": cpu_final,
+                    "max_eig_condition": float(1.0 / max(float(np.min(rc)), 1e-300)),
+                    "rel_diff_final_matrix_gpu_vs_cpu": float(np.linalg.norm(gpu_final_A - X.detach().numpy())
+                                                              / np.linalg.norm(gpu_final_A))})
+    rises = np.array([d["max_re_lambda_after_gpu"] - d["max_re_lambda_before"] for d in out])
+    cpu_rises = np.array([d["max_re_lambda_after_cpu"] - d["max_re_lambda_before"] for d in out])
+    return {"worst": out, "cpu_reproduces_rise": bool(np.all((cpu_rises > 0) == (rises > 0))),
+            "method": f"{worst} largest rises; CPU: torch.linalg.eigvals FP64 + autograd, {steps} steps, lr {lr}"}
 
 
 def measure_ragged(h, dev, stream, peak, batch: int = 200000) -> dict:
@@ -669,11 +740,47 @@ def measure_ragged(h, dev, stream, peak, batch: int = 200000) -> dict:
             assert st == 0
 
     ms_plain = time_ms(per_size_calls, 2, stream)
+    flag2_serial = flag2.clone()
+    eig2_serial = eig2.clone()
+
+    # The same 64 plain launches spread over CONC_STREAMS streams, each stream with its own
+    # handle (so each has its own estimator stream) and its own workspace; sizes are dealt
+    # largest work first to the stream with the least work so far.
+    CONC_STREAMS = 8
+    streams = [torch.cuda.Stream(dev) for _ in range(CONC_STREAMS)]
+    handles = [api.Handle() for _ in range(CONC_STREAMS)]
+    works = [torch.empty(wmax, dtype=torch.uint8, device=dev) for _ in range(CONC_STREAMS)]
+    load = [0.0] * CONC_STREAMS
+    plan = [[] for _ in range(CONC_STREAMS)]
+    for k in sorted((k for k in range(1, 65) if counts[k]), key=lambda k: -float(counts[k]) * k ** 3):
+        i = min(range(CONC_STREAMS), key=lambda i: load[i])
+        plan[i].append(k)
+        load[i] += float(counts[k]) * k ** 3
+
+    def per_size_concurrent():
+        for i in range(CONC_STREAMS):
+            streams[i].wait_stream(stream)
+            for k in plan[i]:
+                p0, e0 = starts[k]
+                st = api.tokura_zgeev_batched_gpu(handles[i], k, int(counts[k]), A.data_ptr() + 16 * p0,
+                                                  eig2.data_ptr() + 16 * e0, works[i].data_ptr(),
+                                                  flag2.data_ptr() + int(fbase[k - 1]), streams[i].cuda_stream)
+                assert st == 0
+        for i in range(CONC_STREAMS):
+            stream.wait_stream(streams[i])
+
+    ms_conc = time_ms(per_size_concurrent, 2, stream)
+    conc_same = bool(torch.equal(flag2, flag2_serial) and torch.equal(eig2, eig2_serial))
+    del works, handles
     work_flops = float(np.sum(40.0 * ns.astype(np.float64) ** 3))
     best = graph_ms if isinstance(graph_ms, float) else ms_ragged
     return {"batch": batch, "total_elements": total, "ms_ragged": ms_ragged, "ms_ragged_graph": graph_ms,
             "ms_per_size_plain": ms_plain, "matrices_per_s_ragged": batch / (best * 1e-3),
             "matrices_per_s_per_size_plain": batch / (ms_plain * 1e-3), "speedup_vs_per_size": ms_plain / best,
+            "ms_per_size_plain_concurrent": ms_conc, "speedup_vs_per_size_concurrent": ms_conc / best,
+            "per_size_concurrent": f"the 64 plain launches over {CONC_STREAMS} streams, one handle and one "
+                                   f"workspace each, sizes dealt largest work first to the least-loaded stream; "
+                                   f"results bitwise equal to the serial launches: {conc_same}",
             "fp64_frac": work_flops / (best * 1e-3) / peak, "flagged": flagged,
             "plain_launches": int(np.count_nonzero(counts)), "parity": parity,
             "shift_hints": "FP32 estimates for orders >= 48 (the default); the per-size plain launches use them "
@@ -978,6 +1085,7 @@ def run_only(args):
 
 
 def main():
+    global CHECK_SUBSET, CHECK_FULL_FLAGS
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
@@ -1001,7 +1109,6 @@ def main():
                     help="LAPACK on every matrix of each batch for flag parity, or on the subset only")
     args = ap.parse_args()
     set_workload(args.n, args.batch)
-    global CHECK_SUBSET, CHECK_FULL_FLAGS
     CHECK_SUBSET = args.check_subset
     CHECK_FULL_FLAGS = args.check_flags == "all"
     if args.impl == "reference":
