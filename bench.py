@@ -615,14 +615,28 @@ def measure_config5(h, dev, stream, peak, batch: int = 20000, steps: int = 100) 
 
 def diagnose_config5(A0, A1, ns, offsets, maxre0, maxre1, tau, lr, steps, worst: int = 10) -> dict:
     """The matrices whose max Re lambda rose most over the GD run: their largest eigenvalue
-    condition number (LAPACK zgeevx on the initial matrix) and the same run of `steps` GD steps
-    repeated on the CPU with torch.linalg.eigvals (FP64) and autograd, per matrix (the loss is
-    a sum over matrices, so each matrix's trajectory is independent)."""
+    condition number (LAPACK zgeevx on the initial matrix); the same `steps` GD steps repeated on
+    the CPU with torch.linalg.eigvals (FP64) and autograd, per matrix (the loss is a sum over
+    matrices, so each matrix's trajectory is independent), once from the same start and once from
+    a start perturbed by 1e-14 relative (the trajectory's sensitivity to rounding); and the CPU's
+    max Re lambda of the GPU's final matrix (the forward at the end point)."""
     import numpy as np
     import torch
 
     from oracle import lapack_oracle as lo
 
+    def run_cpu(M):
+        X = torch.from_numpy(M.copy()).requires_grad_(True)
+        for _ in range(steps):
+            lam = torch.linalg.eigvals(X)
+            loss = tau * torch.logsumexp(lam.real / tau, 0)
+            (g,) = torch.autograd.grad(loss, X)
+            with torch.no_grad():
+                X -= lr * g
+        X = X.detach()
+        return X.numpy(), float(torch.linalg.eigvals(X).real.max())
+
+    rng = np.random.default_rng(5)
     rise = (maxre1 - maxre0).cpu().numpy()
     idx = np.argsort(-rise)[:worst]
     out = []
@@ -631,25 +645,28 @@ def diagnose_config5(A0, A1, ns, offsets, maxre0, maxre1, tau, lr, steps, worst:
         o = int(offsets[j])
         M0 = A0[o:o + k * k].cpu().numpy().reshape(k, k)  # the column-major buffer read row-major: A^T
         _, rc, _ = lo.zgeevx_rconde(M0[None])
-        X = torch.from_numpy(M0.copy()).requires_grad_(True)
-        for _ in range(steps):
-            lam = torch.linalg.eigvals(X)
-            loss = tau * torch.logsumexp(lam.real / tau, 0)
-            (g,) = torch.autograd.grad(loss, X)
-            with torch.no_grad():
-                X -= lr * g
-        with torch.no_grad():
-            cpu_final = float(torch.linalg.eigvals(X).real.max())
+        X, cpu_final = run_cpu(M0)
+        pert = M0 + 1e-14 * np.linalg.norm(M0) / k * (rng.standard_normal(M0.shape) + 1j * rng.standard_normal(M0.shape))
+        Xp, cpu_pert_final = run_cpu(pert)
         gpu_final_A = A1[o:o + k * k].cpu().numpy().reshape(k, k)
+        nrm = np.linalg.norm(gpu_final_A)
         out.append({"n": k, "max_re_lambda_before": float(maxre0[j]), "max_re_lambda_after_gpu": float(maxre1[j]),
-                    "max_re_lambda_after_cpu": cpu_final,
+                    "cpu_max_re_lambda_of_gpu_final_matrix": float(np.linalg.eigvals(gpu_final_A).real.max()),
+                    "max_re_lambda_after_cpu": cpu_final, "max_re_lambda_after_cpu_perturbed_1e-14": cpu_pert_final,
                     "max_eig_condition": float(1.0 / max(float(np.min(rc)), 1e-300)),
-                    "rel_diff_final_matrix_gpu_vs_cpu": float(np.linalg.norm(gpu_final_A - X.detach().numpy())
-                                                              / np.linalg.norm(gpu_final_A))})
+                    "rel_diff_final_matrix_gpu_vs_cpu": float(np.linalg.norm(gpu_final_A - X) / nrm),
+                    "rel_diff_final_matrix_cpu_vs_cpu_perturbed": float(np.linalg.norm(Xp - X) / nrm)})
     rises = np.array([d["max_re_lambda_after_gpu"] - d["max_re_lambda_before"] for d in out])
     cpu_rises = np.array([d["max_re_lambda_after_cpu"] - d["max_re_lambda_before"] for d in out])
+    fwd_ok = all(abs(d["cpu_max_re_lambda_of_gpu_final_matrix"] - d["max_re_lambda_after_gpu"]) <= 1e-8 * max(
+        1.0, abs(d["max_re_lambda_after_gpu"])) for d in out)
     return {"worst": out, "cpu_reproduces_rise": bool(np.all((cpu_rises > 0) == (rises > 0))),
-            "method": f"{worst} largest rises; CPU: torch.linalg.eigvals FP64 + autograd, {steps} steps, lr {lr}"}
+            "gpu_forward_matches_cpu_at_final_matrices": bool(fwd_ok),
+            "median_rel_diff_gpu_vs_cpu": float(np.median([d["rel_diff_final_matrix_gpu_vs_cpu"] for d in out])),
+            "median_rel_diff_cpu_vs_perturbed_cpu": float(np.median(
+                [d["rel_diff_final_matrix_cpu_vs_cpu_perturbed"] for d in out])),
+            "method": f"{worst} largest rises; CPU: torch.linalg.eigvals FP64 + autograd, {steps} steps, lr {lr}; "
+                      f"a rounding-size (1e-14) perturbation of the start tests the trajectory's sensitivity"}
 
 
 def measure_ragged(h, dev, stream, peak, batch: int = 200000) -> dict:
@@ -786,6 +803,79 @@ def measure_ragged(h, dev, stream, peak, batch: int = 200000) -> dict:
             "shift_hints": "FP32 estimates for orders >= 48 (the default); the per-size plain launches use them "
                            "for n >= 12"}
 
+def measure_reference_gpu(h, dev, stream, peak) -> dict:
+    """The reference library itself (tokura_zgeev_batched_library, unmodified, built for sm_103a
+    with the three host functions it declares but never defines restated in
+    oracle/ref_gpu_glue.cu) beside this library, on the same device-resident inputs.
+
+    Its kernels keep block barriers in control flow that diverges between the 32 matrices of a
+    thread block, so they run only on batches where each block of 32 consecutive matrices holds
+    copies of one matrix, and only on matrices that the CPU restatement of its algorithm
+    converges (oracle/ref_gpu.py). Such batches flatter both libraries a little (no divergence
+    between the matrices of a warp); configuration 1 and the main workload are this library's
+    figures on distinct matrices. Orders 32 (313 x 32 = 10,016 matrices, configuration 1's size)
+    and 64 (2,048 x 32 = 65,536, the main workload's size)."""
+    import numpy as np
+    import torch
+
+    from oracle import lapack_oracle as lo
+    from oracle import ref_gpu
+    from tokura_zgeev_batched_gb300 import api, workloads
+
+    if not os.path.exists(ref_gpu.LIB_PATH):
+        return {"unavailable": "reference library not built (its sources were not staged with the tree)"}
+    out = {"method": "each thread block of the reference = 32 copies of one seeded complex Gaussian matrix; "
+                     "CUDA events around one tokura_zgeev_batched_gpu call of each library on the same device batch "
+                     "(the reference overwrites A, so it is re-copied before its call, outside the timing)"}
+    for n, d in ((32, 313), (64, 2048)):
+        cand = workloads.gaussian(d + d // 8 + 8, n, seed=SEED + 60 + n)
+        ok, passes = ref_gpu.safe_matrices(cand, 20)
+        distinct = cand[ok[:d]]
+        d = distinct.shape[0]
+        ref_gpu.solve_uniform(distinct[:8], stream)  # warm-up (module load)
+        # a quarter of the batch first: the full batch only if it is projected to take under a minute
+        q = max(8, d // 4)
+        _, _, ms_q = ref_gpu.solve_uniform(distinct[:q], stream)
+        if ms_q * d / q > 60e3:
+            distinct = distinct[:q]
+            d = q
+        eig_r, flag_r, ms_r = ref_gpu.solve_uniform(distinct, stream)
+        batch = d * 32
+        e = eig_r.view(d, 32, n)
+        copies_identical = bool((e == e[:, :1]).all().item())
+        f = flag_r.view(d, 32)
+        rep = lo.batch_parity(distinct, e[:, 0].cpu().numpy(), f[:, 0].cpu().numpy(), subset=d)
+        # this library on the same batch
+        A = torch.from_numpy(distinct).to(dev).repeat_interleave(32, dim=0)
+        eig = torch.empty(batch, n, dtype=torch.complex128, device=dev)
+        flag = torch.empty(batch, dtype=torch.int8, device=dev)
+        work = torch.empty(api.tokura_get_zgeeveigenvaluesgetworspacesize(n, batch), dtype=torch.uint8, device=dev)
+
+        def ours():
+            assert api.tokura_zgeev_batched_gpu(h, n, batch, A.data_ptr(), eig.data_ptr(), work.data_ptr(),
+                                                flag.data_ptr(), stream.cuda_stream) == 0
+
+        ms_o = time_ms(ours, 3, stream)
+        rep_o = lo.batch_parity(distinct, eig.view(d, 32, n)[:, 0].cpu().numpy(),
+                                flag.view(d, 32)[:, 0].cpu().numpy(), subset=d)
+        out[str(n)] = {
+            "batch": batch, "distinct_matrices": d,
+            "cpu_restatement_passes_max": int(passes[ok[:d]].max()),
+            "reference_ms": ms_r, "reference_matrices_per_s": batch / (ms_r * 1e-3),
+            "reference_fp64_frac": flops_per_matrix(n) * batch / (ms_r * 1e-3) / peak,
+            "reference_flagged": int((flag_r != 0).sum().item()), "reference_copies_identical": copies_identical,
+            "reference_parity": {"max_rel_err_fro": rep["max_rel_err"], "p99_rel_err_fro": rep["p99_rel_err"],
+                                 "max_rel_err_fro_cond_le_1e3": rep["max_rel_err_well"],
+                                 "flag_mismatch": rep["flag_mismatch"], "checked": rep["checked"]},
+            "ours_ms": ms_o, "ours_matrices_per_s": batch / (ms_o * 1e-3),
+            "ours_parity": {"max_rel_err_fro": rep_o["max_rel_err"], "flag_mismatch": rep_o["flag_mismatch"]},
+            "speedup_ours_vs_reference": ms_r / ms_o,
+        }
+        del A, eig, flag, work, eig_r, flag_r
+        torch.cuda.empty_cache()
+    return out
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -812,6 +902,8 @@ def run_ours(args):
 
     peak = api.probe_fp64_peak(dev)
     h = api.Handle()
+    if args.lanes:  # profiling cases: the full-size launch shape on a smaller batch
+        assert h.set_plain_config(N, args.lanes, 32) == 0
     stream = torch.cuda.current_stream(dev)
     s = stream.cuda_stream
 
@@ -1027,6 +1119,12 @@ def run_ours(args):
         torch.cuda.empty_cache()
         phase("eigenvectors done")
 
+    reference_gpu = None
+    if rank == 0 and not args.no_reference_gpu:
+        reference_gpu = guarded(lambda: measure_reference_gpu(h, dev, stream, peak))
+        torch.cuda.empty_cache()
+        phase("reference library on the GPU done")
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         cpu = guarded(lambda: cpu_baseline(N))
@@ -1047,6 +1145,7 @@ def run_ours(args):
             "gpu_launches": args.steps * (3 if N >= SHIFT_HINT_MIN_N else 1), "flagged": flagged, "parity": parity, "sweep": sweep,
             "config1_n32_10000": config1, "ragged": ragged, "config4_backward": config4,
             "config5_ragged_gd_graph": config5, "real_dgeev_n64": real, "eigenvectors_n64": vectors,
+            "reference_gpu": reference_gpu,
         }
         print(json.dumps(out), flush=True)
     if dist is not None:
@@ -1079,6 +1178,8 @@ def run_only(args):
                 raise RuntimeError(f"tokura_zgeev_batched_gpu returned {st}")
 
         out = measure_config1(h, dev, stream, peak, call)
+    elif args.only == "reference_gpu":
+        out = measure_reference_gpu(h, dev, stream, peak)
     else:
         out = measure_config4(h, dev, stream, peak, batch=args.batch or 50000, orders=(args.n,))
     print(json.dumps({"only": args.only, "result": out}), flush=True)
@@ -1099,10 +1200,14 @@ def main():
     ap.add_argument("--no-grad", action="store_true")
     ap.add_argument("--no-real", action="store_true")
     ap.add_argument("--no-vectors", action="store_true")
-    ap.add_argument("--only", choices=["ragged", "backward", "real", "vectors", "config1"], default=None,
+    ap.add_argument("--no-reference-gpu", action="store_true")
+    ap.add_argument("--only", choices=["ragged", "backward", "real", "vectors", "config1", "reference_gpu"],
+                    default=None,
                     help="run one configuration alone (profiling cases); --batch sets its size")
     ap.add_argument("--n", type=int, default=N, help="matrix order of the timed workload (profiling cases)")
     ap.add_argument("--batch", type=int, default=0, help="matrices per GPU (default: 4 GiB of input)")
+    ap.add_argument("--lanes", type=int, default=0, choices=[0, 1, 2, 4, 8],
+                    help="lanes per matrix of the timed workload (profiling cases; 0 = the library's choice)")
     ap.add_argument("--check-subset", type=int, default=CHECK_SUBSET,
                     help="matrices per configuration whose eigenvalues are matched against LAPACK")
     ap.add_argument("--check-flags", choices=["all", "subset"], default="all",

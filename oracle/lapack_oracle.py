@@ -84,6 +84,7 @@ def _load():
             ctypes.c_int, ctypes.POINTER(ctypes.c_double)]
         lib.ref_zgeev_batched.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
                                           ctypes.c_void_p]
+        lib.ref_zgeev_batched_sweeps.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 4
         lib.model_zgeev_batched.argtypes = [ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 5
         lib.model_zgeev_batched_opts.argtypes = ([ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 4
                                                  + [ctypes.c_double] + [ctypes.c_void_p] * 3 + [ctypes.c_int]
@@ -191,18 +192,20 @@ def zgeevx_rconde(A: np.ndarray, threads: int | None = None):
     return w, rc, info
 
 
-def reference_algorithm(A: np.ndarray):
+def reference_algorithm(A: np.ndarray, return_sweeps: bool = False):
     """The reference's own GPU algorithm restated serially in C (oracle/ref_algorithm.c).
 
-    Returns ``(w[batch, n], flag[batch])``; flag 1 means its n^4 sweep cap was hit.
+    Returns ``(w[batch, n], flag[batch])``; flag 1 means its n^4 sweep cap was hit. With
+    ``return_sweeps`` also the passes of its sweep loop per matrix.
     """
     lib = _load()
     A = _as_batch(A)
     b, n, _ = A.shape
     w = np.empty((b, n), np.complex128)
     flag = np.empty(b, np.int32)
-    lib.ref_zgeev_batched(n, b, A.ctypes.data, w.ctypes.data, flag.ctypes.data)
-    return w, flag
+    sweeps = np.empty(b, np.int64)
+    lib.ref_zgeev_batched_sweeps(n, b, A.ctypes.data, w.ctypes.data, flag.ctypes.data, sweeps.ctypes.data)
+    return (w, flag, sweeps) if return_sweeps else (w, flag)
 
 
 def model_qr(A: np.ndarray, est: np.ndarray | None = None):

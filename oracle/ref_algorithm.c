@@ -111,8 +111,10 @@ static int block_end(const int* zi, int n, int i) {
 }
 
 /* Single-shift QR on the Hessenberg matrix (tokura_zhseqr_MWB_kernel.cuh:611-791).
- * Returns the flag (0 converged, 1 sweep cap n^4 reached) and writes w[i]. */
-static int ref_zhseqr(int n, cplx* a, cplx* w) {
+ * Returns the flag (0 converged, 1 sweep cap n^4 reached), writes w[i] and the
+ * number of passes of the kernel's sweep loop (its counter `its`, :654-657) to
+ * *its_out. */
+static int ref_zhseqr(int n, cplx* a, cplx* w, long long* its_out) {
   int* zi = (int*)calloc((size_t)n + 1, sizeof(int));
   zi[n] = n;
   long long cap = (long long)n * n * n * n, its = 0;
@@ -196,6 +198,7 @@ static int ref_zhseqr(int n, cplx* a, cplx* w) {
     }
   }
   int flag = (its == cap) ? 1 : 0;
+  *its_out = its;
   for (int s = n - 1; s >= 0;) {
     if (zi[s] != 0 || s == 0) {
       w[s] = AT(a, n, s, s);
@@ -212,8 +215,9 @@ static int ref_zhseqr(int n, cplx* a, cplx* w) {
   return flag;
 }
 
-/* Reference algorithm on `batch` column-major matrices (A is copied, not modified). */
-int ref_zgeev_batched(int n, int batch, const double* A, double* w, int* flag) {
+/* Reference algorithm on `batch` column-major matrices (A is copied, not
+ * modified); sweeps (may be NULL): passes of the sweep loop per matrix. */
+int ref_zgeev_batched_sweeps(int n, int batch, const double* A, double* w, int* flag, long long* sweeps) {
   cplx* a = (cplx*)malloc(sizeof(cplx) * (size_t)n * n);
   cplx* v = (cplx*)malloc(sizeof(cplx) * (size_t)n);
   if (!a || !v) {
@@ -224,9 +228,15 @@ int ref_zgeev_batched(int n, int batch, const double* A, double* w, int* flag) {
   for (int k = 0; k < batch; ++k) {
     memcpy(a, A + (size_t)k * n * n * 2, sizeof(cplx) * (size_t)n * n);
     ref_zgehrd(n, a, v);
-    flag[k] = ref_zhseqr(n, a, (cplx*)(w + (size_t)k * n * 2));
+    long long its = 0;
+    flag[k] = ref_zhseqr(n, a, (cplx*)(w + (size_t)k * n * 2), &its);
+    if (sweeps) sweeps[k] = its;
   }
   free(a);
   free(v);
   return 0;
+}
+
+int ref_zgeev_batched(int n, int batch, const double* A, double* w, int* flag) {
+  return ref_zgeev_batched_sweeps(n, batch, A, w, flag, NULL);
 }

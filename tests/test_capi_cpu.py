@@ -133,6 +133,7 @@ def test_create_destroy_null(lib):
     assert lib.tokuraSetSweepCap(None, 3) == -1
     assert lib.tokuraSetBalancing(None, 3) == -1
     assert lib.tokuraSetShiftHints(None, 1) == -1
+    assert lib.tokuraSetScaledRotations(None, 24) == -1
     assert lib.tokuraSetHostLinkRate(None, 10.0) == -1
     assert lib.tokuraSetRaggedHintMinOrder(None, 48) == -1
     # Host allocator: argument checks and unknown pointers need no GPU.

@@ -62,6 +62,8 @@ _SIGNATURES = {
     "tokuraSaveTuning": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
     "tokuraSetBalancing": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "tokuraSetShiftHints": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "tokuraSetScaledRotations": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
+    "tokuraDebugAttach": (ctypes.c_int, [ctypes.c_void_p]),
     "tokura_zgeev_vectors_batched_gpu": (
         ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int] + [ctypes.c_void_p] * 7),
     "tokura_get_zgeev_vectors_workspacesize": (ctypes.c_size_t, [ctypes.c_int, ctypes.c_int]),
@@ -104,14 +106,21 @@ def exported_symbols() -> list[str]:
     return list(_SIGNATURES)
 
 
+def debug_bounds_requested() -> bool:
+    """TOKURA_ZGEEV_DEBUG_BOUNDS=1 selects the bounds-checked library (csrc/zgeev_debug.cuh) for
+    this process; it must be set before the first call into the library."""
+    return os.environ.get("TOKURA_ZGEEV_DEBUG_BOUNDS", "0") not in ("", "0")
+
+
 def lib(autobuild: bool = True) -> ctypes.CDLL:
     """Loads (building first if allowed and needed) the C-ABI library."""
     global _LIB
     if _LIB is not None:
         return _LIB
-    path = _build.LIB_PATH
-    if autobuild and _build.needs_build():
-        _build.build()
+    debug = debug_bounds_requested()
+    path = _build.DEBUG_LIB_PATH if debug else _build.LIB_PATH
+    if autobuild and _build.needs_build(debug=debug):
+        _build.build(debug=debug)
     if not os.path.exists(path):
         raise ImportError(f"{path} is missing: build it with tokura_zgeev_batched_gb300.build.build()")
     handle = ctypes.CDLL(path)
@@ -171,6 +180,10 @@ class Handle:
         """FP32 eigenvalue estimates as first shifts: 1 (default) uniform batches with n >= 12,
         2 every entry point and order (ragged too), 0 off (Wilkinson shifts only)."""
         return int(lib().tokuraSetShiftHints(self.ptr, int(mode)))
+
+    def set_scaled_rotations(self, min_order: int) -> int:
+        """Plain QR with scaled rotations from this order on (7..64; 65 = never)."""
+        return int(lib().tokuraSetScaledRotations(self.ptr, int(min_order)))
 
     def set_real_config(self, n: int, lanes: int, threads: int) -> int:
         return int(lib().tokuraSetRealConfig(self.ptr, int(n), int(lanes), int(threads)))

@@ -22,6 +22,10 @@ INCLUDE = os.path.join(REPO_DIR, "include")
 BUILD_DIR = os.path.join(PKG_DIR, "_build")
 LIB_NAME = "libtokura_zgeev_gb300.so"
 LIB_PATH = os.path.join(PKG_DIR, LIB_NAME)
+# Bounds-checked build (-DTOKURA_DEBUG_BOUNDS, csrc/zgeev_debug.cuh): a separate library.
+DEBUG_BUILD_DIR = os.path.join(PKG_DIR, "_build_debug")
+DEBUG_LIB_PATH = os.path.join(PKG_DIR, "libtokura_zgeev_gb300_debug.so")
+DEBUG_FLAGS = ["-DTOKURA_DEBUG_BOUNDS"]
 
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-fvisibility=hidden", "--expt-relaxed-constexpr"]
@@ -38,6 +42,7 @@ SOURCES = [
     "tokura_tuner.cu",
     "zgeev_backward.cu",
     "zgeev_vectors.cu",
+    "zgeev_debug.cu",
     "tokura_capi.cpp",
     "compat_cxx.cpp",
     "tokura_host_pipeline.cpp",
@@ -63,20 +68,25 @@ def _all_inputs() -> list[str]:
     return files
 
 
-def needs_build(extra: list[str] | None = None) -> bool:
-    extra = extra or []
-    stamp = os.path.join(BUILD_DIR, "flags.sha1")
-    if not os.path.exists(LIB_PATH) or not os.path.exists(stamp):
+def _paths(debug: bool) -> tuple[str, str]:
+    return (DEBUG_BUILD_DIR, DEBUG_LIB_PATH) if debug else (BUILD_DIR, LIB_PATH)
+
+
+def needs_build(extra: list[str] | None = None, debug: bool = False) -> bool:
+    extra = list(extra or []) + (DEBUG_FLAGS if debug else [])
+    build_dir, lib_path = _paths(debug)
+    stamp = os.path.join(build_dir, "flags.sha1")
+    if not os.path.exists(lib_path) or not os.path.exists(stamp):
         return True
     with open(stamp) as f:
         if f.read().strip() != _flags_digest(extra):
             return True
-    lib_mtime = os.path.getmtime(LIB_PATH)
+    lib_mtime = os.path.getmtime(lib_path)
     return any(os.path.getmtime(p) > lib_mtime for p in _all_inputs())
 
 
-def _compile(src: str, extra: list[str]) -> str:
-    obj = os.path.join(BUILD_DIR, os.path.basename(src) + ".o")
+def _compile(src: str, extra: list[str], build_dir: str = BUILD_DIR) -> str:
+    obj = os.path.join(build_dir, os.path.basename(src) + ".o")
     cmd = [_nvcc(), "-c", os.path.join(CSRC, src), "-o", obj, "-I", INCLUDE, "-I", CSRC] + ARCH_FLAGS + NVCC_FLAGS + extra
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
@@ -84,26 +94,28 @@ def _compile(src: str, extra: list[str]) -> str:
     return obj
 
 
-def build(force: bool = False, extra: list[str] | None = None, verbose: bool = False) -> str:
-    """Compiles the library if needed and returns its path."""
-    extra = list(extra or [])
-    if not force and not needs_build(extra):
-        return LIB_PATH
-    os.makedirs(BUILD_DIR, exist_ok=True)
-    with cf.ThreadPoolExecutor(max_workers=min(8, len(SOURCES))) as ex:
-        objs = list(ex.map(lambda s: _compile(s, extra), SOURCES))
-    tmp = LIB_PATH + ".tmp"
+def build(force: bool = False, extra: list[str] | None = None, verbose: bool = False, debug: bool = False) -> str:
+    """Compiles the library if needed and returns its path (``debug``: the bounds-checked
+    library, a separate file)."""
+    if not force and not needs_build(extra, debug):
+        return _paths(debug)[1]
+    extra = list(extra or []) + (DEBUG_FLAGS if debug else [])
+    build_dir, lib_path = _paths(debug)
+    os.makedirs(build_dir, exist_ok=True)
+    with cf.ThreadPoolExecutor(max_workers=min(max(os.cpu_count() or 8, 8), len(SOURCES))) as ex:
+        objs = list(ex.map(lambda s: _compile(s, extra, build_dir), SOURCES))
+    tmp = lib_path + ".tmp"
     cmd = [_nvcc(), "-shared", "-o", tmp] + objs + ARCH_FLAGS + ["-Xcompiler", "-fPIC"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
-    os.replace(tmp, LIB_PATH)
-    with open(os.path.join(BUILD_DIR, "flags.sha1"), "w") as f:
+    os.replace(tmp, lib_path)
+    with open(os.path.join(build_dir, "flags.sha1"), "w") as f:
         f.write(_flags_digest(extra))
     if verbose:
-        print(f"built {LIB_PATH}", file=sys.stderr)
-    return LIB_PATH
+        print(f"built {lib_path}", file=sys.stderr)
+    return lib_path
 
 
 if __name__ == "__main__":
-    build(force="--force" in sys.argv, verbose=True)
+    build(force="--force" in sys.argv, verbose=True, debug="--debug" in sys.argv)

@@ -20,7 +20,13 @@ struct RMatView {
   double* p;
   int n;
   int rs;
-  __device__ __forceinline__ double* at(int r, int c) const { return p + (c * n + r) * rs; }
+  __device__ __forceinline__ double* at(int r, int c) const {
+#ifdef TOKURA_DEBUG_BOUNDS
+    if (dbg_out(r, c, n)) return p;
+#endif
+    return p + (c * n + r) * rs;
+  }
+  __device__ __forceinline__ double* ptr(int r, int c) const { return p + (c * n + r) * rs; }
 };
 
 struct SrcReal64 {
@@ -461,14 +467,18 @@ __device__ int real_qr_eigenvalues(const RMatView& M, const Group<L>& G, Out* __
       const double t2 = t1 * v2, t3 = t1 * v3;
       if (nr == 3) {
         // rows k..k+2 of columns k..i, then columns k..k+2 of rows l..min(k+3, i)
-        reflect_triples<3>(M.at(k, k + G.rank), strided_count(k + G.rank, i, L), L * cs, rs, v2, v3, t1, t2, t3);
+        TZG_DBG_RUN(M, k, k + G.rank, 0, L, strided_count(k + G.rank, i, L), 2, 0);
+        reflect_triples<3>(M.ptr(k, k + G.rank), strided_count(k + G.rank, i, L), L * cs, rs, v2, v3, t1, t2, t3);
         G.sync();
-        reflect_triples<3>(M.at(l + G.rank, k), strided_count(l + G.rank, min(k + 3, i), L), L * rs, cs, v2, v3, t1,
+        TZG_DBG_RUN(M, l + G.rank, k, L, 0, strided_count(l + G.rank, min(k + 3, i), L), 0, 2);
+        reflect_triples<3>(M.ptr(l + G.rank, k), strided_count(l + G.rank, min(k + 3, i), L), L * rs, cs, v2, v3, t1,
                            t2, t3);
       } else {
-        reflect_triples<2>(M.at(k, k + G.rank), strided_count(k + G.rank, i, L), L * cs, rs, v2, 0.0, t1, t2, 0.0);
+        TZG_DBG_RUN(M, k, k + G.rank, 0, L, strided_count(k + G.rank, i, L), 1, 0);
+        reflect_triples<2>(M.ptr(k, k + G.rank), strided_count(k + G.rank, i, L), L * cs, rs, v2, 0.0, t1, t2, 0.0);
         G.sync();
-        reflect_triples<2>(M.at(l + G.rank, k), strided_count(l + G.rank, i, L), L * rs, cs, v2, 0.0, t1, t2, 0.0);
+        TZG_DBG_RUN(M, l + G.rank, k, L, 0, strided_count(l + G.rank, i, L), 0, 1);
+        reflect_triples<2>(M.ptr(l + G.rank, k), strided_count(l + G.rank, i, L), L * rs, cs, v2, 0.0, t1, t2, 0.0);
       }
       G.sync();
     }

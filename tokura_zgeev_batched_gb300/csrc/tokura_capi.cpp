@@ -149,7 +149,7 @@ extern "C" int tokura_zgeev_ragged_gpu(tokurablas_t* handle, int batch_count, co
                                              total_elements, reinterpret_cast<const double2*>(A),
                                              reinterpret_cast<double2*>(eigenvalues), work, flag,
                                              handle->itmax_override, stream, handle->balance_mode,
-                                             tzg::ragged_hint_min_order(handle), &handle->fj);
+                                             tzg::ragged_hint_min_order(handle), &handle->fj, handle->scaled_min_n);
   return err == cudaSuccess ? 0 : 1;
 }
 
@@ -263,6 +263,13 @@ extern "C" int tokuraSetBalancing(tokurablas_t* handle, int mode) {
   if (handle == nullptr) return -1;
   if (mode < 0 || mode > 3) return -2;
   handle->balance_mode = mode;
+  return 0;
+}
+
+extern "C" int tokuraSetScaledRotations(tokurablas_t* handle, int min_order) {
+  if (handle == nullptr) return -1;
+  if (!(min_order >= 7 && min_order <= TOKURA_ZGEEV_BATCHED_MAX_MATRIX_SIZE + 1)) return -2;
+  handle->scaled_min_n = min_order;
   return 0;
 }
 

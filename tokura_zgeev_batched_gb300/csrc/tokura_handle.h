@@ -25,6 +25,12 @@ struct HostPipeline {
 
 }  // namespace tzg
 
+namespace tzg {
+// Default smallest order of the plain QR with scaled rotations.
+constexpr int kScaledRotationDefaultMinN = 16;
+}  // namespace tzg
+using tzg::kScaledRotationDefaultMinN;
+
 struct tokurablas_t {
   int device = 0;
   int sm_count = 0;
@@ -35,6 +41,7 @@ struct tokurablas_t {
   int ragged_lanes = 0;  // lanes per matrix of the ragged solvers; 0 = chosen per launch
   int balance_mode = 0;  // balancing before the eigenvalue solves: 0 none (the reference's behaviour) .. 3 both
   int ragged_hint_min_n = 48;  // mode 1: ragged matrices of this order and above get hints (65: none)
+  int scaled_min_n = kScaledRotationDefaultMinN;  // plain QR with scaled rotations from this order (65: never)
   int shift_hints = 1;   // FP32 eigenvalue estimates as first shifts: 0 off, 1 uniform batches with
                          // n >= kShiftHintMinN, 2 every eigenvalue entry point and order (ragged too)
   tzg::HostPipeline pipe;  // host-buffer entry point state (guarded by pipe_mutex)
@@ -72,6 +79,7 @@ inline PlainConfig plain_config_for(const tokurablas_t* h, int n, int batch) {
     if (n <= 2) c.lanes = 1;
   }
   if (c.threads == 0) c.threads = 32;
+  c.scaled = (n >= h->scaled_min_n && n >= 7) ? 1 : 0;
   return c;
 }
 

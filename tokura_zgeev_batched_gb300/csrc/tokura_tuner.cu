@@ -107,7 +107,8 @@ extern "C" TOKURA_API int tokuraAutotune(tokurablas_t* handle, int n_min, int n_
     for (int li = 0; li < 4; ++li) {
       if (n <= 2 && kLanes[li] > 1) continue;
       for (int ti = 0; ti < 4; ++ti) {
-        const PlainConfig cfg{kLanes[li], kThreads[ti]};
+        PlainConfig cfg{kLanes[li], kThreads[ti]};
+        cfg.scaled = plain_config_for(handle, n, batch_count).scaled;
         cudaError_t err;
         const float ms = time_launches(stream, 2, [&]() {
           return launch_plain(cfg, n, batch_count, A, eig, work, flag, default_itmax(n), stream, 0,
@@ -152,7 +153,7 @@ extern "C" TOKURA_API int tokuraAutotuneRagged(tokurablas_t* handle, int batch_c
     const float ms = time_launches(stream, 2, [&]() {
       return launch_ragged(lanes, handle->sm_count, batch_count, n, off, nullptr, total, A,
                            static_cast<double2*>(b.p[1]), b.p[2], static_cast<char*>(b.p[3]), 0, stream, 0,
-                           ragged_hint_min_order(handle), &handle->fj);
+                           ragged_hint_min_order(handle), &handle->fj, handle->scaled_min_n);
     }, &err);
     if (err != cudaSuccess) return 1;
     if (ms < best) {

@@ -62,10 +62,13 @@ __device__ void form_q(const BwdViews& V, const Group<L>& G) {
     int c = r + 1 + G.rank;
     for (; c + L < n; c += 2 * L) {
       double2* p[2] = {Q.at(r + 1, c), Q.at(r + 1, c + L)};
+      TZG_DBG_TOUCH(Q, r + m, c + L);
+      TZG_DBG_TOUCH(T, r + m, r);
       reflect_vectors<2, false>(p, x, m, rs, rs, tau);
     }
     if (c < n) {
       double2* p[1] = {Q.at(r + 1, c)};
+      TZG_DBG_TOUCH(Q, r + m, c);
       reflect_vectors<1, false>(p, x, m, rs, rs, tau);
     }
     G.sync();
@@ -172,18 +175,22 @@ __device__ int schur_qr(const BwdViews& V, const Group<L>& G, const double2* __r
       G.sync();
       if (j > lo && G.rank == 0) *T.at(j, j - 1) = rr;
       // Left: rows (j, j+1), columns j .. n-1.
-      rotate_pairs<false>(g, T.at(j, j + G.rank), strided_count(j + G.rank, n - 1, L), L * cs, rs);
+      TZG_DBG_RUN(T, j, j + G.rank, 0, L, strided_count(j + G.rank, n - 1, L), 1, 0);
+      rotate_pairs<false>(g, T.ptr(j, j + G.rank), strided_count(j + G.rank, n - 1, L), L * cs, rs);
       G.sync();
       // Right: columns (j, j+1), rows 0 .. min(j+1, i); bulge row j+2; and Q's rows 0 .. n-1.
       const int qend = min(j + 1, i);
-      rotate_pairs<true>(g, T.at(G.rank, j), strided_count(G.rank, qend, L), L * rs, cs);
+      TZG_DBG_RUN(T, G.rank, j, L, 0, strided_count(G.rank, qend, L), 0, 1);
+      rotate_pairs<true>(g, T.ptr(G.rank, j), strided_count(G.rank, qend, L), L * rs, cs);
       if (j + 2 <= i && G.rank == ((j + 2) & (L - 1))) {
         double2* pb = T.at(j + 2, j);
+        TZG_DBG_TOUCH(T, j + 2, j + 1);
         const double2 b = pb[cs];
         pb[0] = make_double2(fma(g.s.x, b.x, g.s.y * b.y), fma(g.s.x, b.y, -g.s.y * b.x));
         pb[cs] = make_double2(g.c * b.x, g.c * b.y);
       }
-      rotate_pairs<true>(g, Q.at(G.rank, j), strided_count(G.rank, n - 1, L), L * rs, cs);
+      TZG_DBG_RUN(Q, G.rank, j, L, 0, strided_count(G.rank, n - 1, L), 0, 1);
+      rotate_pairs<true>(g, Q.ptr(G.rank, j), strided_count(G.rank, n - 1, L), L * rs, cs);
       G.sync();
     }
   }

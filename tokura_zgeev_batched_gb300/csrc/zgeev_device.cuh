@@ -22,6 +22,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "zgeev_debug.cuh"
+
 namespace tzg {
 
 constexpr int kMaxN = 64;
@@ -114,7 +116,15 @@ struct MatView {
   double2* p;
   int n;
   int rs;  // stride between consecutive rows (= tile width)
-  __device__ __forceinline__ double2* at(int r, int c) const { return p + (c * n + r) * rs; }
+  __device__ __forceinline__ double2* at(int r, int c) const {
+#ifdef TOKURA_DEBUG_BOUNDS
+    if (dbg_out(r, c, n)) return p;
+#endif
+    return p + (c * n + r) * rs;
+  }
+  // Start of a strided run that may be empty (not checked: a run is checked by
+  // TZG_DBG_RUN on its first and last elements when it has any).
+  __device__ __forceinline__ double2* ptr(int r, int c) const { return p + (c * n + r) * rs; }
 };
 
 // Complex Givens rotation G = [c s; -conj(s) c] (c real) with G * [x; y] = [rr; 0].

@@ -111,7 +111,12 @@ struct SMat {
   float2* p;
   int n;
   int ld;
-  __device__ __forceinline__ float2* at(int r, int c) const { return p + c * ld + r; }
+  __device__ __forceinline__ float2* at(int r, int c) const {
+#ifdef TOKURA_DEBUG_BOUNDS
+    if (dbg_out(r, c, n)) return p;
+#endif
+    return p + c * ld + r;
+  }
 };
 
 __device__ __forceinline__ bool negligible_f(const SMat& S, int k, int lo, int hi, float smlnum) {

@@ -13,6 +13,7 @@ namespace tzg {
 struct PlainConfig {
   int lanes;            // lanes per matrix: 1, 2, 4 or 8
   int threads;          // threads per block (multiple of 32)
+  int scaled = 0;       // QR with scaled rotations (orders >= 7; zgeev_scaled_qr.cuh)
 };
 
 // Iteration cap per eigenvalue: LAPACK's rule 30*max(10, n) unless overridden.
@@ -43,7 +44,7 @@ size_t ragged_workspace_bytes(int batch, long long total_elements);
 cudaError_t launch_ragged(int lanes, int sms, int batch, const int* n, const long long* offsets,
                           const long long* eig_offsets, long long total_elements, const double2* A, double2* eig,
                           void* work, char* flag, int itmax_override, cudaStream_t stream, int balance = 0,
-                          int hint_min_n = 0, const ForkJoin* fj = nullptr);
+                          int hint_min_n = 0, const ForkJoin* fj = nullptr, int scaled_min_n = 65);
 
 // Backward (Abar from A, eigenvalues and their gradients).
 size_t backward_workspace_bytes(int n, int batch);

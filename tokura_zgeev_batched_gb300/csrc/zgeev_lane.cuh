@@ -306,6 +306,7 @@ __device__ void hessenberg(const MatView& M, const Group<L>& G, double2* tau_out
       alpha = make_double2(-xn, 0.0);
       tau = 1.0;
     }
+    TZG_DBG_TOUCH(M, r + m, r);  // last entry of the reflector vector
     for (int i = 1 + G.rank; i < m; i += L) x[i * rs] = cmul(x[i * rs], cg);
     G.sync();
     if (G.rank == 0) {
@@ -317,10 +318,12 @@ __device__ void hessenberg(const MatView& M, const Group<L>& G, double2* tau_out
       int c = r + 1 + G.rank;
       for (; c + L < n; c += 2 * L) {
         double2* p[2] = {M.at(r + 1, c), M.at(r + 1, c + L)};
+        TZG_DBG_TOUCH(M, r + m, c + L);
         reflect_vectors<2, false>(p, x, m, rs, rs, tau);
       }
       if (c < n) {
         double2* p[1] = {M.at(r + 1, c)};
+        TZG_DBG_TOUCH(M, r + m, c);
         reflect_vectors<1, false>(p, x, m, rs, rs, tau);
       }
     }
@@ -330,10 +333,12 @@ __device__ void hessenberg(const MatView& M, const Group<L>& G, double2* tau_out
       int q = G.rank;
       for (; q + L < n; q += 2 * L) {
         double2* p[2] = {M.at(q, r + 1), M.at(q + L, r + 1)};
+        TZG_DBG_TOUCH(M, q + L, r + m);
         reflect_vectors<2, true>(p, x, m, cs, rs, tau);
       }
       if (q < n) {
         double2* p[1] = {M.at(q, r + 1)};
+        TZG_DBG_TOUCH(M, q, r + m);
         reflect_vectors<1, true>(p, x, m, cs, rs, tau);
       }
     }
@@ -395,7 +400,7 @@ __device__ __forceinline__ bool negligible_subdiag(const MatView& M, int k, int 
 // sweep cap defaults to LAPACK's 30*max(10, n).
 template <int L, class Out = double2>
 __device__ int qr_eigenvalues(const MatView& M, const Group<L>& G, Out* __restrict__ eig_out, int shift, int itmax,
-                              const float2* __restrict__ est = nullptr) {
+                              const float2* __restrict__ est = nullptr, int* sweeps_out = nullptr) {
   const int n = M.n;
   const int rs = M.rs;
   const int cs = n * rs;
@@ -407,6 +412,7 @@ __device__ int qr_eigenvalues(const MatView& M, const Group<L>& G, Out* __restri
   int its = 0;     // sweeps since the last deflation (LAPACK's per-eigenvalue cap)
   int kdefl = 0;   // sweeps since the last deflation, for ad hoc shifts
   unsigned long long used = 0;  // estimates already matched to a deflated eigenvalue
+  int sweeps = 0;               // sweeps of this matrix (reported when sweeps_out is given)
   // One loop iteration = (deflations, then) one sweep. Lanes of a warp hold
   // different matrices; keeping them in lockstep per sweep rather than per
   // eigenvalue means a lane whose eigenvalue converged early goes straight
@@ -446,6 +452,7 @@ __device__ int qr_eigenvalues(const MatView& M, const Group<L>& G, Out* __restri
     }
     ++its;
     ++kdefl;
+    ++sweeps;
     {
       // Shift selection.
       double2 sigma;
@@ -481,7 +488,8 @@ __device__ int qr_eigenvalues(const MatView& M, const Group<L>& G, Out* __restri
         // Left: rows (j, j+1), columns j .. i.
         {
           const int c0 = j + G.rank;
-          rotate_pairs<false>(g, M.at(j, c0), strided_count(c0, i, L), L * cs, rs);
+          TZG_DBG_RUN(M, j, c0, 0, L, strided_count(c0, i, L), 1, 0);
+          rotate_pairs<false>(g, M.ptr(j, c0), strided_count(c0, i, L), L * cs, rs);
         }
         G.sync();
         // Right: columns (j, j+1), rows lo .. min(j+2, i); row j+2 holds the
@@ -489,9 +497,11 @@ __device__ int qr_eigenvalues(const MatView& M, const Group<L>& G, Out* __restri
         {
           const int qend = min(j + 1, i);
           const int q0 = lo + G.rank;
-          rotate_pairs<true>(g, M.at(q0, j), strided_count(q0, qend, L), L * rs, cs);
+          TZG_DBG_RUN(M, q0, j, L, 0, strided_count(q0, qend, L), 0, 1);
+          rotate_pairs<true>(g, M.ptr(q0, j), strided_count(q0, qend, L), L * rs, cs);
           if (j + 2 <= i && G.rank == ((j + 2 - lo) & (L - 1))) {
             double2* pb = M.at(j + 2, j);
+            TZG_DBG_TOUCH(M, j + 2, j + 1);
             const double2 b = pb[cs];
             // a' = conj(s) b ; b' = c b
             pb[0] = make_double2(fma(g.s.x, b.x, g.s.y * b.y), fma(g.s.x, b.y, -g.s.y * b.x));
@@ -509,6 +519,7 @@ __device__ int qr_eigenvalues(const MatView& M, const Group<L>& G, Out* __restri
       put_ev(eig_out + k, make_double2(d.x * unscale, d.y * unscale));
     }
   }
+  if (sweeps_out != nullptr) *sweeps_out = sweeps;
   return status;
 }
 

@@ -34,6 +34,7 @@
 #include "zgeev_estimate.cuh"
 #include "zgeev_internal.h"
 #include "zgeev_lane.cuh"
+#include "zgeev_scaled_qr.cuh"
 
 namespace tzg {
 
@@ -79,10 +80,13 @@ struct Complex64Batch {
   __device__ __forceinline__ float2* out(long long j, int) const { return W + j * n; }
 };
 
+// `scaled` (nonzero, n >= kScaledMinN) selects the QR with scaled rotations
+// (zgeev_scaled_qr.cuh) for the QR part; the prepare part does not depend on it.
 template <int L, bool kBalance, int kPhase, class Batch>
 __global__ void __launch_bounds__(256) zgeev_plain_kernel(int n, int batch, Batch B, double2* __restrict__ work,
                                                            char* __restrict__ flag, int itmax, int balance,
-                                                           const float2* __restrict__ est, int* __restrict__ state) {
+                                                           const float2* __restrict__ est, int* __restrict__ state,
+                                                           int scaled) {
   constexpr int TW = 32 / L;
   const int lane = threadIdx.x & 31;
   const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -105,9 +109,21 @@ __global__ void __launch_bounds__(256) zgeev_plain_kernel(int n, int batch, Batc
     }
     return;
   }
+#ifdef TOKURA_DEBUG_BOUNDS
+  int sweeps = -1;
+  int* const sw = &sweeps;
+  TZG_DBG_INDEX(j, batch);
+#else
+  int* const sw = nullptr;
+#endif
   if (kPhase == kPhaseAll) {
-    const int status = solve_matrix<L, kBalance>(B.src(j), M, G, B.out(j, n), itmax, balance,
-                                                 est != nullptr ? est + j * n : nullptr);
+    int shift;
+    int status = prepare_matrix<L, kBalance>(B.src(j), M, G, B.out(j, n), balance, shift);
+    if (status == kPrepared) {
+      const float2* e = est != nullptr ? est + j * n : nullptr;
+      status = (scaled != 0 && n >= kScaledMinN) ? qr_eigenvalues_scaled<L>(M, G, B.out(j, n), shift, itmax, e, sw)
+                                                 : qr_eigenvalues<L>(M, G, B.out(j, n), shift, itmax, e, sw);
+    }
     if (G.rank == 0) flag[j] = (char)status;
   } else if (kPhase == kPhasePrepare) {
     int shift;
@@ -119,22 +135,27 @@ __global__ void __launch_bounds__(256) zgeev_plain_kernel(int n, int batch, Batc
   } else {
     const int s = state[j];
     if (s == kStateDone) return;  // group-uniform
-    const int status = qr_eigenvalues<L>(M, G, B.out(j, n), s, itmax, est + j * n);
+    const int status = (scaled != 0 && n >= kScaledMinN)
+                           ? qr_eigenvalues_scaled<L>(M, G, B.out(j, n), s, itmax, est + j * n, sw)
+                           : qr_eigenvalues<L>(M, G, B.out(j, n), s, itmax, est + j * n, sw);
     if (G.rank == 0) flag[j] = (char)status;
   }
+#ifdef TOKURA_DEBUG_BOUNDS
+  if (kPhase != kPhasePrepare && G.rank == 0 && sweeps >= 0) dbg_record_sweeps(j, sweeps);
+#endif
 }
 
 template <int L, bool kBalance, int kPhase, class Batch>
 inline cudaError_t launch_plain_l(unsigned blocks, int threads, cudaStream_t stream, int n, int batch,
                                   const Batch& B, double2* work, char* flag, int itmax, int balance,
-                                  const float2* est, int* state, int carveout) {
+                                  const float2* est, int* state, int carveout, int scaled) {
   if (kPhase != kPhaseAll) {  // shared memory for estimators running beside (this or another call's)
     const cudaError_t err = cudaFuncSetAttribute(zgeev_plain_kernel<L, kBalance, kPhase, Batch>,
                                                  cudaFuncAttributePreferredSharedMemoryCarveout, carveout);
     if (err != cudaSuccess) return err;
   }
   zgeev_plain_kernel<L, kBalance, kPhase, Batch>
-      <<<blocks, threads, 0, stream>>>(n, batch, B, work, flag, itmax, balance, est, state);
+      <<<blocks, threads, 0, stream>>>(n, batch, B, work, flag, itmax, balance, est, state, scaled);
   return cudaGetLastError();
 }
 
@@ -143,31 +164,31 @@ inline cudaError_t launch_plain_l(unsigned blocks, int threads, cudaStream_t str
 template <int kPhase, class Batch>
 inline cudaError_t launch_plain_phase(int L, bool bal, unsigned blocks, int threads, cudaStream_t stream, int n,
                                       int batch, const Batch& B, double2* work, char* flag, int itmax, int balance,
-                                      const float2* est, int* state, int carveout = cudaSharedmemCarveoutDefault) {
+                                      const float2* est, int* state, int carveout, int scaled) {
   constexpr bool kB = kPhase != kPhaseQR;  // balanced instantiation exists
   const bool b = bal && kB;
   const int bv = b ? balance : 0;
   switch (L) {
     case 1:
       return b ? launch_plain_l<1, kB, kPhase>(blocks, threads, stream, n, batch, B, work, flag, itmax, bv, est, state,
-                                                        carveout)
+                                                        carveout, scaled)
                : launch_plain_l<1, false, kPhase>(blocks, threads, stream, n, batch, B, work, flag, itmax, 0, est, state,
-                                                           carveout);
+                                                           carveout, scaled);
     case 2:
       return b ? launch_plain_l<2, kB, kPhase>(blocks, threads, stream, n, batch, B, work, flag, itmax, bv, est, state,
-                                                        carveout)
+                                                        carveout, scaled)
                : launch_plain_l<2, false, kPhase>(blocks, threads, stream, n, batch, B, work, flag, itmax, 0, est, state,
-                                                           carveout);
+                                                           carveout, scaled);
     case 4:
       return b ? launch_plain_l<4, kB, kPhase>(blocks, threads, stream, n, batch, B, work, flag, itmax, bv, est, state,
-                                                        carveout)
+                                                        carveout, scaled)
                : launch_plain_l<4, false, kPhase>(blocks, threads, stream, n, batch, B, work, flag, itmax, 0, est, state,
-                                                           carveout);
+                                                           carveout, scaled);
     case 8:
       return b ? launch_plain_l<8, kB, kPhase>(blocks, threads, stream, n, batch, B, work, flag, itmax, bv, est, state,
-                                                        carveout)
+                                                        carveout, scaled)
                : launch_plain_l<8, false, kPhase>(blocks, threads, stream, n, batch, B, work, flag, itmax, 0, est, state,
-                                                           carveout);
+                                                           carveout, scaled);
     default:
       return cudaErrorInvalidValue;
   }
@@ -188,16 +209,18 @@ cudaError_t launch_batch(const PlainConfig& cfg, int n, int batch, const Batch& 
   const long long blocks = (warps * 32 + threads - 1) / threads;
   if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
   const bool bal = balance != 0;
+  const int scaled = cfg.scaled;
+  constexpr int kDef = cudaSharedmemCarveoutDefault;
   if (!hints)
     return launch_plain_phase<kPhaseAll>(L, bal, (unsigned)blocks, threads, stream, n, batch, B, work, flag, itmax,
-                                         balance, nullptr, nullptr);
+                                         balance, nullptr, nullptr, kDef, scaled);
   float2* est = reinterpret_cast<float2*>(work + (size_t)n * n * batch);
   int* state = reinterpret_cast<int*>(est + (size_t)n * batch);
   cudaError_t err;
   if (fj == nullptr || fj->aux == nullptr) {  // no second stream: estimator first, then one kernel
     if ((err = launch_estimates(n, batch, B, est, stream)) != cudaSuccess) return err;
     return launch_plain_phase<kPhaseAll>(L, bal, (unsigned)blocks, threads, stream, n, batch, B, work, flag, itmax,
-                                         balance, est, nullptr);
+                                         balance, est, nullptr, kDef, scaled);
   }
   std::lock_guard<std::mutex> lock(*fj->mu);
   if ((err = cudaEventRecord(fj->fork, stream)) != cudaSuccess) return err;
@@ -205,12 +228,13 @@ cudaError_t launch_batch(const PlainConfig& cfg, int n, int batch, const Batch& 
   if ((err = launch_estimates(n, batch, B, est, fj->aux)) != cudaSuccess) return err;
   if ((err = cudaEventRecord(fj->join, fj->aux)) != cudaSuccess) return err;
   if ((err = launch_plain_phase<kPhasePrepare>(L, bal, (unsigned)blocks, threads, stream, n, batch, B, work, flag,
-                                               itmax, balance, nullptr, state, cudaSharedmemCarveoutMaxShared)) !=
+                                               itmax, balance, nullptr, state, cudaSharedmemCarveoutMaxShared,
+                                               scaled)) !=
       cudaSuccess)
     return err;
   if ((err = cudaStreamWaitEvent(stream, fj->join, 0)) != cudaSuccess) return err;
   return launch_plain_phase<kPhaseQR>(L, false, (unsigned)blocks, threads, stream, n, batch, B, work, flag, itmax, 0,
-                                      est, state, cudaSharedmemCarveoutMaxShared);
+                                      est, state, cudaSharedmemCarveoutMaxShared, scaled);
 }
 
 }  // namespace tzg

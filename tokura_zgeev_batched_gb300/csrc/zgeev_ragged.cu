@@ -171,7 +171,7 @@ static cudaError_t ragged_prepare(int lanes, int sms, int batch, const int* n, c
 cudaError_t launch_ragged(int lanes, int sms, int batch, const int* n, const long long* offsets,
                           const long long* eig_offsets, long long total_elements, const double2* A, double2* eig,
                           void* work, char* flag, int itmax_override, cudaStream_t stream, int balance,
-                          int hint_min_n, const ForkJoin* fj) {
+                          int hint_min_n, const ForkJoin* fj, int scaled_min_n) {
   // Shift hints for the matrices of order >= hint_min_n (0: none).
   const bool hints = hint_min_n > 0 && hint_min_n <= kMaxN;
   if (lanes == 0) lanes = ragged_auto_lanes(sms, batch, total_elements);
@@ -198,7 +198,7 @@ cudaError_t launch_ragged(int lanes, int sms, int batch, const int* n, const lon
                        &sorted, &eo);
   if (err != cudaSuccess) return err;
   const RaggedArgs args{offsets, eo, A, eig, nullptr, nullptr, nullptr, stage, total_elements, flag, sorted,
-                        itmax_override, balance, est, state, hint_min_n};
+                        itmax_override, balance, est, state, hint_min_n, scaled_min_n};
   if (split) return ragged_launch_phases(lanes, sms, plan, args, balance != 0, stream, *fj);
   if (balance != 0) return launch_ragged_kernel<false, true, kPhaseAll>(lanes, sms, plan, args, stream);
   return launch_ragged_kernel<false, false, kPhaseAll>(lanes, sms, plan, args, stream);

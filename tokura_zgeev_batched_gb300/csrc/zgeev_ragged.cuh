@@ -8,6 +8,7 @@
 #include "zgeev_estimate.cuh"
 #include "zgeev_internal.h"
 #include "zgeev_lane.cuh"
+#include "zgeev_scaled_qr.cuh"
 
 namespace tzg {
 
@@ -88,6 +89,7 @@ struct RaggedArgs {
   const float2* est;     // forward: FP32 shift hints, kMaxN per matrix (or null)
   int* state;            // forward, split solve: pre-scaling exponent or kStateDone per matrix
   int est_min_n;         // forward: orders from which est holds hints
+  int scaled_min_n = 65;  // forward: orders from which the QR uses scaled rotations (zgeev_scaled_qr.cuh)
 };
 
 // Tile scheduling. Tiles are numbered in descending-work order; SM s owns
@@ -151,8 +153,14 @@ __global__ void __launch_bounds__(128) zgeev_ragged_kernel(RaggedPlan* plan, Rag
         status = backward_matrix<L>(a.A + a.offsets[j], a.lam + a.eoff[j], a.gbar + a.eoff[j],
                                     a.gA + a.offsets[j], V, G, itmax);
       } else if (kPhase == kPhaseAll) {
-        status = solve_matrix<L, kBalance>(a.A + a.offsets[j], MatView{base, nb, tw}, G, a.eig + a.eoff[j], itmax,
-                                           a.balance, est);
+        int shift;
+        const MatView M{base, nb, tw};
+        status = prepare_matrix<L, kBalance>(SrcContig{a.A + a.offsets[j]}, M, G, a.eig + a.eoff[j], a.balance,
+                                             shift);
+        if (status == kPrepared)
+          status = (nb >= a.scaled_min_n && nb >= kScaledMinN)
+                       ? qr_eigenvalues_scaled<L>(M, G, a.eig + a.eoff[j], shift, itmax, est)
+                       : qr_eigenvalues<L>(M, G, a.eig + a.eoff[j], shift, itmax, est);
       } else if (kPhase == kPhasePrepare) {
         int shift;
         status = prepare_matrix<L, kBalance>(SrcContig{a.A + a.offsets[j]}, MatView{base, nb, tw}, G,
@@ -161,7 +169,9 @@ __global__ void __launch_bounds__(128) zgeev_ragged_kernel(RaggedPlan* plan, Rag
       } else {
         const int s = a.state[j];
         if (s != kStateDone)
-          status = qr_eigenvalues<L>(MatView{base, nb, tw}, G, a.eig + a.eoff[j], s, itmax, est);
+          status = (nb >= a.scaled_min_n && nb >= kScaledMinN)
+                       ? qr_eigenvalues_scaled<L>(MatView{base, nb, tw}, G, a.eig + a.eoff[j], s, itmax, est)
+                       : qr_eigenvalues<L>(MatView{base, nb, tw}, G, a.eig + a.eoff[j], s, itmax, est);
       }
       if (G.rank == 0 && status != kPrepared) a.flag[j] = (char)status;
     }
