@@ -52,17 +52,20 @@ TOKURA_API int tokuraSetBalancing(tokurablas_t* handle, int mode);
  * Returns 0, -1 NULL handle, -2 bad mode. */
 TOKURA_API int tokuraSetShiftHints(tokurablas_t* handle, int mode);
 
-/* Smallest order from which the eigenvalue calls (plain, strided,
- * pointer-array, complex64, host-buffer, workspace-free and ragged entry
- * points) run the QR with scaled rotations: the Hessenberg matrix is kept with real row
- * and column scale factors, which makes each rotation update two complex
+/* Orders from which the eigenvalue calls (plain, strided, pointer-array,
+ * complex64, host-buffer, workspace-free and ragged entry points), the
+ * gradients (plain and ragged backward) and the eigenvector call run their QR
+ * with scaled rotations, per lane: with L lanes per matrix (the launch shape),
+ * orders n >= max(7, L * min_order). The Hessenberg matrix is kept with real
+ * row and column scale factors, which makes each rotation update two complex
  * multiply-adds per element pair (8 FP64 instructions instead of 12) at the
  * same rounding-error bound; the factors live in matrix entries the QR does
- * not use, so the workspace is unchanged. 7..64; 65 = never; default 16
- * (n = 64: -10 % call time, n = 32: -5 %, n = 16: -0.6 %; below 16 the
- * per-rotation bookkeeping outweighs the savings). Results keep
- * the FP64 accuracy either way but are not bitwise identical.
- * Returns 0, -1 NULL handle, -2 order outside 7..65. */
+ * not use, so the workspace is unchanged. min_order 1..64; 65 = never;
+ * default 16 (1 lane: n = 64 -10 % call time, 32 -5 %, 16 -0.6 %; 4 lanes at
+ * n = 32: +9 %, since a rotation's fixed cost is paid per lane group while its
+ * savings shrink with the pairs each lane updates). Results keep the FP64
+ * accuracy either way but are not bitwise identical.
+ * Returns 0, -1 NULL handle, -2 min_order outside 1..65. */
 TOKURA_API int tokuraSetScaledRotations(tokurablas_t* handle, int min_order);
 
 /* Smallest order whose matrices get shift hints in ragged calls under mode 1

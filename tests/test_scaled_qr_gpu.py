@@ -13,7 +13,7 @@ pytestmark = pytest.mark.gpu
 GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "zgeev_golden.npz")
 
 
-def solve(A_np, min_order=7, hints=1, lanes=0, cap=0):
+def solve(A_np, min_order=1, hints=1, lanes=0, cap=0):
     import torch
     from tokura_zgeev_batched_gb300 import api
 
@@ -35,8 +35,8 @@ def test_setter_validation(cuda):
     from tokura_zgeev_batched_gb300 import api
 
     h = api.Handle()
-    assert h.set_scaled_rotations(7) == 0 and h.set_scaled_rotations(64) == 0 and h.set_scaled_rotations(65) == 0
-    assert h.set_scaled_rotations(6) == -2 and h.set_scaled_rotations(66) == -2
+    assert h.set_scaled_rotations(1) == 0 and h.set_scaled_rotations(64) == 0 and h.set_scaled_rotations(65) == 0
+    assert h.set_scaled_rotations(0) == -2 and h.set_scaled_rotations(66) == -2
 
 
 @pytest.mark.parametrize("lanes", [1, 2, 4, 8])
@@ -82,7 +82,7 @@ def test_golden_fixtures(cuda, lanes):
 def test_matches_plain_rotations(cuda):
     """Same eigenvalues as the plain rotations to the parity tolerance (not bitwise)."""
     A = wl.gaussian(500, 48, seed=3400)
-    w_s, f_s = solve(A, min_order=7)
+    w_s, f_s = solve(A, min_order=1)
     w_p, f_p = solve(A, min_order=65)
     assert (f_s == 0).all() and (f_p == 0).all()
     fro = np.linalg.norm(A, axis=(1, 2))
@@ -102,7 +102,7 @@ def test_badly_scaled_entries(cuda):
     d = 2.0 ** rng.integers(-20, 21, size=(batch, n))
     A = d[:, :, None] * B / d[:, None, :]
     h = api.Handle()
-    assert h.set_scaled_rotations(7) == 0 and h.set_balancing(3) == 0
+    assert h.set_scaled_rotations(1) == 0 and h.set_balancing(3) == 0
     w, f = api.zgeev_batched(torch.from_numpy(A).cuda(), handle=h)
     w, f = w.cpu().numpy(), f.cpu().numpy()
     w_ref = lo.zgeev(B)[0]
@@ -115,3 +115,50 @@ def test_sweep_cap_sets_flag(cuda):
     w, f = solve(A, cap=1)
     assert (f == 1).all()
     assert np.all(np.isfinite(w))
+
+
+@pytest.mark.parametrize("lanes", [1, 4])
+@pytest.mark.parametrize("n", [7, 24, 48])
+def test_gradient_schur_scaled_and_plain(cuda, n, lanes):
+    """The backward's Schur recomputation with scaled rotations gives torch's gradient, as
+    the plain rotations do."""
+    import torch
+
+    from tokura_zgeev_batched_gb300 import api
+    from tokura_zgeev_batched_gb300.autograd import eigvals
+
+    A_np = wl.vdv(24, n, seed=3700 + n, min_sep=0.05)
+    Ac = torch.from_numpy(A_np).clone().requires_grad_(True)
+    lam = torch.linalg.eigvals(Ac)
+    torch.sum(torch.exp(lam.real) + lam.real ** 2 + lam.imag ** 2).backward()
+    ref = Ac.grad.numpy()
+    for min_order in (1, 65):
+        h = api.Handle()
+        assert h.set_scaled_rotations(min_order) == 0 and h.set_plain_config(n, lanes, 64) == 0
+        A = torch.from_numpy(A_np).cuda().requires_grad_(True)
+        lam_g, flag = eigvals(A, handle=h, return_flag=True)
+        torch.sum(torch.exp(lam_g.real) + lam_g.real ** 2 + lam_g.imag ** 2).backward()
+        g = A.grad.cpu().numpy()
+        assert (flag.cpu().numpy() == 0).all()
+        err = np.linalg.norm(g - ref, axis=(1, 2)) / np.linalg.norm(ref, axis=(1, 2))
+        assert err.max() < 1e-9, (min_order, err.max())
+
+
+@pytest.mark.parametrize("n", [9, 33, 64])
+def test_eigenvectors_scaled_and_plain(cuda, n):
+    import torch
+
+    from tokura_zgeev_batched_gb300 import api
+
+    M = wl.gaussian(24, n, seed=3800 + n)
+    fro = np.linalg.norm(M, axis=(1, 2))
+    for min_order in (1, 65):
+        h = api.Handle()
+        assert h.set_scaled_rotations(min_order) == 0
+        w, VL, VR, f = api.zgeev_vectors(torch.from_numpy(M).cuda(), handle=h)
+        w, VL, VR, f = w.cpu().numpy(), VL.cpu().numpy(), VR.cpu().numpy(), f.cpu().numpy()
+        assert (f == 0).all()
+        for k in range(M.shape[0]):
+            assert np.abs(M[k] @ VR[k] - VR[k] * w[k][None, :]).max() <= 1e-12 * n * fro[k]
+            assert np.abs(VL[k].conj().T @ M[k] - w[k][:, None] * VL[k].conj().T).max() <= 1e-12 * n * fro[k]
+            assert np.allclose(np.linalg.norm(VR[k], axis=0), 1.0, atol=1e-13)

@@ -182,7 +182,7 @@ class Handle:
         return int(lib().tokuraSetShiftHints(self.ptr, int(mode)))
 
     def set_scaled_rotations(self, min_order: int) -> int:
-        """Plain QR with scaled rotations from this order on (7..64; 65 = never)."""
+        """QR with scaled rotations from order max(7, lanes * min_order) on (1..64; 65 = never)."""
         return int(lib().tokuraSetScaledRotations(self.ptr, int(min_order)))
 
     def set_real_config(self, n: int, lanes: int, threads: int) -> int:

@@ -199,7 +199,7 @@ extern "C" int tokura_zgeev_backward_gpu(tokurablas_t* handle, int n, int batch_
   const cudaError_t err = tzg::launch_backward(
       lanes, n, batch_count, reinterpret_cast<const double2*>(A), reinterpret_cast<const double2*>(eigenvalues),
       reinterpret_cast<const double2*>(grad_eigenvalues), reinterpret_cast<double2*>(grad_A),
-      static_cast<double2*>(work), flag, itmax, stream);
+      static_cast<double2*>(work), flag, itmax, stream, tzg::scaled_threshold(handle, lanes));
   return err == cudaSuccess ? 0 : 1;
 }
 
@@ -229,7 +229,7 @@ extern "C" int tokura_zgeev_ragged_backward_gpu(tokurablas_t* handle, int batch_
       handle->ragged_lanes, handle->sm_count, batch_count, n, offsets, eig_offsets, total_elements,
       reinterpret_cast<const double2*>(A), reinterpret_cast<const double2*>(eigenvalues),
       reinterpret_cast<const double2*>(grad_eigenvalues), reinterpret_cast<double2*>(grad_A), work, flag,
-      handle->itmax_override, stream);
+      handle->itmax_override, stream, handle->scaled_min_n);
   return err == cudaSuccess ? 0 : 1;
 }
 
@@ -255,7 +255,7 @@ extern "C" int tokura_zgeev_vectors_batched_gpu(tokurablas_t* handle, int n, int
   const cudaError_t err = tzg::launch_vectors(
       lanes, n, batch_count, reinterpret_cast<const double2*>(A), reinterpret_cast<double2*>(eigenvalues),
       reinterpret_cast<double2*>(VL), reinterpret_cast<double2*>(VR), static_cast<double2*>(work), flag, itmax, stream,
-      tzg::use_shift_hints(handle, n), &handle->fj);
+      tzg::use_shift_hints(handle, n), &handle->fj, tzg::scaled_threshold(handle, lanes));
   return err == cudaSuccess ? 0 : 1;
 }
 
@@ -268,7 +268,7 @@ extern "C" int tokuraSetBalancing(tokurablas_t* handle, int mode) {
 
 extern "C" int tokuraSetScaledRotations(tokurablas_t* handle, int min_order) {
   if (handle == nullptr) return -1;
-  if (!(min_order >= 7 && min_order <= TOKURA_ZGEEV_BATCHED_MAX_MATRIX_SIZE + 1)) return -2;
+  if (!(min_order >= 1 && min_order <= TOKURA_ZGEEV_BATCHED_MAX_MATRIX_SIZE + 1)) return -2;
   handle->scaled_min_n = min_order;
   return 0;
 }

@@ -66,6 +66,17 @@ inline void init_default_tuning(tokurablas_t* h) {
 // 11 % faster in 32- or 64-thread blocks than in 128-thread blocks; with
 // shift hints, 32-thread blocks are 5-9 % faster than 64 at batches of
 // 8,000-20,000 and equal at 65,536).
+// Smallest order that takes the QR with scaled rotations at `lanes` lanes per
+// matrix: lanes * min_order, at least 7 (65: never). The rotation's fixed cost
+// is paid per lane group while its savings scale with the pairs each lane
+// updates (about n / lanes): 10,000 matrices at n = 32 on 4 lanes ran 9 %
+// slower with scaled rotations, 262,144 on 1 lane 5 % faster.
+inline int scaled_threshold(const tokurablas_t* h, int lanes) {
+  if (h->scaled_min_n > 64) return 65;
+  const int t = h->scaled_min_n * (lanes > 0 ? lanes : 1);
+  return t < 7 ? 7 : (t > 65 ? 65 : t);
+}
+
 inline PlainConfig plain_config_for(const tokurablas_t* h, int n, int batch) {
   PlainConfig c = h->plain[n];
   if (c.lanes == 0) {
@@ -79,7 +90,7 @@ inline PlainConfig plain_config_for(const tokurablas_t* h, int n, int batch) {
     if (n <= 2) c.lanes = 1;
   }
   if (c.threads == 0) c.threads = 32;
-  c.scaled = (n >= h->scaled_min_n && n >= 7) ? 1 : 0;
+  c.scaled = n >= scaled_threshold(h, c.lanes) ? 1 : 0;
   return c;
 }
 

@@ -108,7 +108,7 @@ extern "C" TOKURA_API int tokuraAutotune(tokurablas_t* handle, int n_min, int n_
       if (n <= 2 && kLanes[li] > 1) continue;
       for (int ti = 0; ti < 4; ++ti) {
         PlainConfig cfg{kLanes[li], kThreads[ti]};
-        cfg.scaled = plain_config_for(handle, n, batch_count).scaled;
+        cfg.scaled = n >= scaled_threshold(handle, cfg.lanes) ? 1 : 0;
         cudaError_t err;
         const float ms = time_launches(stream, 2, [&]() {
           return launch_plain(cfg, n, batch_count, A, eig, work, flag, default_itmax(n), stream, 0,

@@ -28,6 +28,7 @@
 #pragma once
 
 #include "zgeev_lane.cuh"
+#include "zgeev_scaled_qr.cuh"
 
 namespace tzg {
 
@@ -197,6 +198,198 @@ __device__ int schur_qr(const BwdViews& V, const Group<L>& G, const double2* __r
   return status;
 }
 
+// schur_qr with scaled rotations (zgeev_scaled_qr.cuh): T = K * u_r * v_c and
+// Q = KQ * v_c (Q's columns rotate with T's, so they share the column factors).
+// Full-width updates as schur_qr: left over columns j .. n-1, right over rows
+// 0 .. min(j+1, i) of T and all rows of Q; rescales cover those live ranges.
+// On return T's upper triangle and Q hold true values again (also when the
+// sweep cap is hit), so the eigenvector and gradient steps are unchanged.
+template <int L>
+__device__ int schur_qr_scaled(const BwdViews& V, const Group<L>& G, const double2* __restrict__ lam,
+                               const double2* __restrict__ gbar, double lam_scale, int itmax,
+                               const float2* __restrict__ est = nullptr) {
+  const double tol = lam != nullptr ? kGradDeflationTol : kUlp;
+  const MatView& T = V.T;
+  const MatView& Q = V.Q;
+  const int n = T.n, rs = T.rs, cs = n * rs;
+  const double smlnum = kSafeMin * ((double)n / kUlp);
+  for (int k = G.rank; k < n; k += L) *scale_slot(T, k) = make_double2(1.0, 1.0);
+  G.sync();
+  unsigned long long used = 0ull;
+  int status = kConverged;
+  int i = n - 1, lo = 0, its = 0, kdefl = 0;
+  while (true) {
+    for (;;) {
+      int hit = lo;
+      for (int k = i - G.rank; k > lo; k -= L) {
+        if (negligible_subdiag_scaled(T, k, lo, i, smlnum, tol)) {
+          hit = k;
+          break;
+        }
+      }
+      lo = G.imax(hit);
+      if (lo < i) {
+        // the split entry lies outside the rows the left rotations update (see qr_eigenvalues_scaled)
+        if (lo > 0 && G.rank == 0) *T.at(lo, lo - 1) = make_double2(0.0, 0.0);
+        break;
+      }
+      if (lam != nullptr) {
+        const int kb = nearest_unused(lam, n, used, true_entry(T, i, i), lam_scale);
+        used |= 1ull << kb;
+        if (G.rank == 0) V.vec[i * V.vs] = gbar[kb];
+      } else if (est != nullptr) {
+        const int kb = nearest_estimate(est, n, used, true_entry(T, i, i));
+        if (kb >= 0) used |= 1ull << kb;
+      }
+      i -= 1;
+      lo = 0;
+      its = 0;
+      kdefl = 0;
+      if (i < 0) break;
+    }
+    if (i < 0) break;
+    if (its > itmax) {
+      status = kNotConverged;
+      break;
+    }
+    double2 sigma;
+    const double2 wk = wilkinson_shift(true_entry(T, i - 1, i - 1), true_entry(T, i - 1, i), true_entry(T, i, i - 1),
+                                       true_entry(T, i, i));
+    int kb_est;
+    if (its == 0 && lam != nullptr) {
+      const double2 l = lam[nearest_unused(lam, n, used, wk, lam_scale)];
+      sigma = make_double2(l.x * lam_scale, l.y * lam_scale);
+      if (!(isfinite(sigma.x) && isfinite(sigma.y))) sigma = wk;
+    } else if (its == 0 && est != nullptr && (kb_est = nearest_estimate(est, n, used, wk)) >= 0) {
+      const float2 e = est[kb_est];
+      sigma = make_double2((double)e.x, (double)e.y);
+    } else if ((kdefl + 1) % (2 * kExceptionalPeriod) == 0) {
+      const double2 d = true_entry(T, i, i);
+      sigma = make_double2(d.x + kExceptionalWeight * cabs1(true_entry(T, i, i - 1)), d.y);
+    } else if ((kdefl + 1) % kExceptionalPeriod == 0) {
+      const double2 d = true_entry(T, lo, lo);
+      sigma = make_double2(d.x + kExceptionalWeight * cabs1(true_entry(T, lo + 1, lo)), d.y);
+    } else {
+      sigma = wk;
+    }
+    ++its;
+    ++kdefl;
+    const double2 f0 = *scale_slot(T, lo);
+    double u0 = f0.x, v0 = f0.y, vp = 1.0;
+    for (int j = lo; j < i; ++j) {
+      const double2 f1 = *scale_slot(T, j + 1);
+      double u1 = f1.x, v1 = f1.y;
+      double2 x, y, rr;
+      if (j == lo) {
+        x = csub(cscale(*T.at(lo, lo), u0 * v0), sigma);
+        y = cscale(*T.at(lo + 1, lo), u1 * v0);
+      } else {
+        x = cscale(*T.at(j, j - 1), u0 * vp);
+        y = cscale(*T.at(j + 1, j - 1), u1 * vp);
+      }
+      const Rot g = make_rot(x, y, rr);
+      G.sync();
+      const int c0 = j + G.rank;
+      const int ccount = strided_count(c0, n - 1, L);
+      const int qend = min(j + 1, i);
+      const int tcount = strided_count(G.rank, qend, L);
+      const int qcount = strided_count(G.rank, n - 1, L);
+      if (g.c != 0.0) {
+        const double rl = 1.0 / (g.c * u0 * u1);
+        const double2 alpha = cscale(g.s, u1 * u1 * rl);
+        const double2 beta = make_double2(-g.s.x * (u0 * u0 * rl), g.s.y * (u0 * u0 * rl));
+        if (j > lo && G.rank == 0) {
+          double2* pk = T.at(j, j - 1);
+          TZG_DBG_TOUCH(T, j + 1, j - 1);
+          *pk = cmadd(*pk, alpha, pk[rs]);
+        }
+        TZG_DBG_RUN(T, j, c0, 0, L, ccount, 1, 0);
+        scaled_pairs(alpha, beta, T.ptr(j, c0), ccount, L * cs, rs);
+        u0 *= g.c;
+        u1 *= g.c;
+        G.sync();
+        const double rr2 = 1.0 / (g.c * v0 * v1);
+        const double2 gamma = make_double2(g.s.x * (v1 * v1 * rr2), -g.s.y * (v1 * v1 * rr2));
+        const double2 delta = cscale(g.s, -(v0 * v0 * rr2));
+        TZG_DBG_RUN(T, G.rank, j, L, 0, tcount, 0, 1);
+        scaled_pairs(gamma, delta, T.ptr(G.rank, j), tcount, L * rs, cs);
+        if (j + 2 <= i && G.rank == ((j + 2) & (L - 1))) {
+          double2* pb = T.at(j + 2, j);
+          TZG_DBG_TOUCH(T, j + 2, j + 1);
+          pb[0] = cmul(gamma, pb[cs]);
+        }
+        TZG_DBG_RUN(Q, G.rank, j, L, 0, qcount, 0, 1);
+        scaled_pairs(gamma, delta, Q.ptr(G.rank, j), qcount, L * rs, cs);
+        v0 *= g.c;
+        v1 *= g.c;
+      } else {
+        const double2 sc = make_double2(g.s.x, -g.s.y), msc = make_double2(-g.s.x, g.s.y);
+        const double2 ms = make_double2(-g.s.x, -g.s.y);
+        if (j > lo && G.rank == 0) {
+          double2* pk = T.at(j, j - 1);
+          TZG_DBG_TOUCH(T, j + 1, j - 1);
+          *pk = cmul(g.s, pk[rs]);
+        }
+        TZG_DBG_RUN(T, j, c0, 0, L, ccount, 1, 0);
+        swap_pairs(g.s, msc, T.ptr(j, c0), ccount, L * cs, rs);
+        { const double t = u0; u0 = u1; u1 = t; }
+        G.sync();
+        TZG_DBG_RUN(T, G.rank, j, L, 0, tcount, 0, 1);
+        swap_pairs(sc, ms, T.ptr(G.rank, j), tcount, L * rs, cs);
+        if (j + 2 <= i && G.rank == ((j + 2) & (L - 1))) {
+          double2* pb = T.at(j + 2, j);
+          TZG_DBG_TOUCH(T, j + 2, j + 1);
+          pb[0] = cmul(sc, pb[cs]);
+          pb[cs] = make_double2(0.0, 0.0);
+        }
+        TZG_DBG_RUN(Q, G.rank, j, L, 0, qcount, 0, 1);
+        swap_pairs(sc, ms, Q.ptr(G.rank, j), qcount, L * rs, cs);
+        { const double t = v0; v0 = v1; v1 = t; }
+      }
+      G.sync();
+      if (u0 < kScaleFloor || u1 < kScaleFloor || v0 < kScaleFloor || v1 < kScaleFloor) {
+        // live ranges: row r at columns max(0, r-2) .. n-1; column c of T at rows 0 .. min(c+2, i)
+        // (the bulge at c+2) and of Q at every row.
+        if (u0 < kScaleFloor) {
+          for (int c = max(0, j - 2) + G.rank; c < n; c += L) *T.at(j, c) = cscale(*T.at(j, c), u0);
+          u0 = 1.0;
+        }
+        if (u1 < kScaleFloor) {
+          for (int c = max(0, j - 1) + G.rank; c < n; c += L) *T.at(j + 1, c) = cscale(*T.at(j + 1, c), u1);
+          u1 = 1.0;
+        }
+        G.sync();
+        if (v0 < kScaleFloor) {
+          for (int r = G.rank; r <= min(j + 2, i); r += L) *T.at(r, j) = cscale(*T.at(r, j), v0);
+          for (int r = G.rank; r < n; r += L) *Q.at(r, j) = cscale(*Q.at(r, j), v0);
+          v0 = 1.0;
+        }
+        if (v1 < kScaleFloor) {
+          for (int r = G.rank; r <= min(j + 3, i); r += L) *T.at(r, j + 1) = cscale(*T.at(r, j + 1), v1);
+          for (int r = G.rank; r < n; r += L) *Q.at(r, j + 1) = cscale(*Q.at(r, j + 1), v1);
+          v1 = 1.0;
+        }
+        G.sync();
+      }
+      if (G.rank == 0) *scale_slot(T, j) = make_double2(u0, v0);
+      vp = v0;
+      u0 = u1;
+      v0 = v1;
+    }
+    if (G.rank == 0) *scale_slot(T, i) = make_double2(u0, v0);
+    G.sync();
+  }
+  // True values back into T's upper triangle and Q (column c owned by rank c mod L).
+  G.sync();
+  for (int c = G.rank; c < n; c += L) {
+    const double2 fc = *scale_slot(T, c);
+    for (int r = 0; r <= c; ++r) *T.at(r, c) = cscale(*T.at(r, c), scale_slot(T, r)->x * fc.y);
+    for (int r = 0; r < n; ++r) *Q.at(r, c) = cscale(*Q.at(r, c), fc.y);
+  }
+  G.sync();
+  return status;
+}
+
 // Divides s by d with |d| clamped from below by smin (marks `close`).
 __device__ __forceinline__ double2 div_clamped(double2 s, double2 d, double smin, bool& close) {
   if (cabs1(d) < smin) {
@@ -334,7 +527,7 @@ __device__ void assemble_gradient(const BwdViews& V, const Group<L>& G, double2*
 template <int L>
 __device__ int backward_matrix(const double2* __restrict__ src, const double2* __restrict__ lam,
                                const double2* __restrict__ gbar, double2* __restrict__ gA, const BwdViews& V,
-                               const Group<L>& G, int itmax) {
+                               const Group<L>& G, int itmax, int scaled_min_n = kMaxN + 1) {
   const int n = V.T.n;
   bool nonfinite, zero;
   const int shift = stage_and_scale<L>(src, V.T, G, nonfinite, zero);
@@ -347,7 +540,8 @@ __device__ int backward_matrix(const double2* __restrict__ src, const double2* _
   G.sync();
   form_q<L>(V, G);
   const double lam_scale = shift == 0 ? 1.0 : (shift > 1022 ? 0.5 * pow2(-1022) : pow2(-shift));
-  const int status = schur_qr<L>(V, G, lam, gbar, lam_scale, itmax);
+  const int status = (n >= scaled_min_n && n >= kScaledMinN) ? schur_qr_scaled<L>(V, G, lam, gbar, lam_scale, itmax)
+                                                            : schur_qr<L>(V, G, lam, gbar, lam_scale, itmax);
   if (status != kConverged) {
     const double nan = __longlong_as_double(0x7ff8000000000000LL);
     for (int e = G.rank; e < n * n; e += L) gA[e] = make_double2(nan, nan);

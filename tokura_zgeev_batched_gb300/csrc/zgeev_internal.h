@@ -44,22 +44,23 @@ size_t ragged_workspace_bytes(int batch, long long total_elements);
 cudaError_t launch_ragged(int lanes, int sms, int batch, const int* n, const long long* offsets,
                           const long long* eig_offsets, long long total_elements, const double2* A, double2* eig,
                           void* work, char* flag, int itmax_override, cudaStream_t stream, int balance = 0,
-                          int hint_min_n = 0, const ForkJoin* fj = nullptr, int scaled_min_n = 65);
+                          int hint_min_n = 0, const ForkJoin* fj = nullptr, int scaled_min_n = 65);  // per lane
 
 // Backward (Abar from A, eigenvalues and their gradients).
 size_t backward_workspace_bytes(int n, int batch);
 cudaError_t launch_backward(int lanes, int n, int batch, const double2* A, const double2* lam, const double2* gbar,
-                            double2* gA, double2* work, char* flag, int itmax, cudaStream_t stream);
+                            double2* gA, double2* work, char* flag, int itmax, cudaStream_t stream,
+                            int scaled_min_n = 65);
 size_t ragged_backward_workspace_bytes(int batch, long long total_elements);
 cudaError_t launch_ragged_backward(int lanes, int sms, int batch, const int* n, const long long* offsets,
                                    const long long* eig_offsets, long long total_elements, const double2* A,
                                    const double2* lam, const double2* gbar, double2* gA, void* work, char* flag,
-                                   int itmax_override, cudaStream_t stream);
+                                   int itmax_override, cudaStream_t stream, int scaled_min_n = 65);
 
 // Eigenvalues with eigenvectors (workspace: backward_workspace_bytes).
 cudaError_t launch_vectors(int lanes, int n, int batch, const double2* A, double2* w, double2* VL, double2* VR,
                            double2* work, char* flag, int itmax, cudaStream_t stream, bool hints = false,
-                           const ForkJoin* fj = nullptr);
+                           const ForkJoin* fj = nullptr, int scaled_min_n = 65);
 size_t vectors_workspace_bytes(int n, int batch);
 
 }  // namespace tzg

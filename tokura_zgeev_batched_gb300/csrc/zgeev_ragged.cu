@@ -197,8 +197,10 @@ cudaError_t launch_ragged(int lanes, int sms, int batch, const int* n, const lon
   err = ragged_prepare(lanes, sms, batch, n, offsets, eig_offsets, total_elements, lay, work, flag, stream, &plan,
                        &sorted, &eo);
   if (err != cudaSuccess) return err;
+  // scaled_min_n is per lane: orders >= lanes * scaled_min_n (at least 7; 65 or more: never)
+  const int scaled_from = scaled_min_n > 64 ? 65 : max(7, min(65, scaled_min_n * lanes));
   const RaggedArgs args{offsets, eo, A, eig, nullptr, nullptr, nullptr, stage, total_elements, flag, sorted,
-                        itmax_override, balance, est, state, hint_min_n, scaled_min_n};
+                        itmax_override, balance, est, state, hint_min_n, scaled_from};
   if (split) return ragged_launch_phases(lanes, sms, plan, args, balance != 0, stream, *fj);
   if (balance != 0) return launch_ragged_kernel<false, true, kPhaseAll>(lanes, sms, plan, args, stream);
   return launch_ragged_kernel<false, false, kPhaseAll>(lanes, sms, plan, args, stream);
@@ -207,7 +209,7 @@ cudaError_t launch_ragged(int lanes, int sms, int batch, const int* n, const lon
 cudaError_t launch_ragged_backward(int lanes, int sms, int batch, const int* n, const long long* offsets,
                                    const long long* eig_offsets, long long total_elements, const double2* A,
                                    const double2* lam, const double2* gbar, double2* gA, void* work, char* flag,
-                                   int itmax_override, cudaStream_t stream) {
+                                   int itmax_override, cudaStream_t stream, int scaled_min_n) {
   if (lanes == 0) lanes = ragged_auto_lanes(sms, batch, total_elements);
   if (!(lanes == 1 || lanes == 2 || lanes == 4 || lanes == 8)) return cudaErrorInvalidValue;
   const RaggedLayout lay = ragged_layout(batch, total_elements, 4);
@@ -218,8 +220,9 @@ cudaError_t launch_ragged_backward(int lanes, int sms, int batch, const int* n, 
   cudaError_t err = ragged_prepare(lanes, sms, batch, n, offsets, eig_offsets, total_elements, lay, work, flag,
                                    stream, &plan, &sorted, &eo);
   if (err != cudaSuccess) return err;
+  const int scaled_from = scaled_min_n > 64 ? 65 : max(7, min(65, scaled_min_n * lanes));
   const RaggedArgs args{offsets, eo, A, nullptr, lam, gbar, gA, stage, total_elements, flag, sorted, itmax_override,
-                        0, nullptr, nullptr, 0};
+                        0, nullptr, nullptr, 0, scaled_from};
   return launch_ragged_kernel<true, false, kPhaseAll>(lanes, sms, plan, args, stream);
 }
 

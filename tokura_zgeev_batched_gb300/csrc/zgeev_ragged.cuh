@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(128) zgeev_ragged_kernel(RaggedPlan* plan, Rag
         BwdViews V{MatView{base, nb, tw}, MatView{base + a.region, nb, tw}, MatView{base + 2 * a.region, nb, tw},
                    base + 3 * a.region, tw};
         status = backward_matrix<L>(a.A + a.offsets[j], a.lam + a.eoff[j], a.gbar + a.eoff[j],
-                                    a.gA + a.offsets[j], V, G, itmax);
+                                    a.gA + a.offsets[j], V, G, itmax, a.scaled_min_n);
       } else if (kPhase == kPhaseAll) {
         int shift;
         const MatView M{base, nb, tw};

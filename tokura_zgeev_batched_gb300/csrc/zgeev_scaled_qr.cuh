@@ -80,8 +80,10 @@ __device__ __forceinline__ void swap_pairs(double2 fa, double2 fb, double2* p, i
   }
 }
 
-// Deflation test of negligible_subdiag on the true entries K * u * v.
-__device__ __forceinline__ bool negligible_subdiag_scaled(const MatView& M, int k, int lo, int hi, double smlnum) {
+// Deflation test of negligible_subdiag on the true entries K * u * v (tol:
+// relative threshold, as negligible_subdiag's).
+__device__ __forceinline__ bool negligible_subdiag_scaled(const MatView& M, int k, int lo, int hi, double smlnum,
+                                                          double tol = kUlp) {
   const double2 sk = *scale_slot(M, k), sk1 = *scale_slot(M, k - 1);
   const double h1 = cabs1(*M.at(k, k - 1)) * (sk.x * sk1.y);
   if (h1 <= smlnum) return true;
@@ -92,14 +94,14 @@ __device__ __forceinline__ bool negligible_subdiag_scaled(const MatView& M, int 
     if (k - 2 >= lo) tst += cabs1(*M.at(k - 1, k - 2)) * (sk1.x * scale_slot(M, k - 2)->y);
     if (k + 1 <= hi) tst += cabs1(*M.at(k + 1, k)) * (scale_slot(M, k + 1)->x * sk.y);
   }
-  if (h1 > kUlp * tst) return false;
+  if (h1 > tol * tst) return false;
   const double hu = cabs1(*M.at(k - 1, k)) * (sk1.x * sk.y);
   const double ab = fmax(h1, hu), ba = fmin(h1, hu);
   const double dd = cabs1(csub(dk1, dkk));
   const double d1 = cabs1(dkk);
   const double aa = fmax(d1, dd), bb = fmin(d1, dd);
   const double s = aa + ab;
-  return ba * (ab / s) <= fmax(smlnum, kUlp * (bb * (aa / s)));
+  return ba * (ab / s) <= fmax(smlnum, tol * (bb * (aa / s)));
 }
 
 // True entry H(r, c).

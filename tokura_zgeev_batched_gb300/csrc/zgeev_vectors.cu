@@ -78,9 +78,10 @@ __device__ int vectors_prepare(const double2* __restrict__ src, double2* __restr
 template <int L>
 __device__ int vectors_finish(double2* __restrict__ w_out, double2* __restrict__ VL, double2* __restrict__ VR,
                               const BwdViews& V, const Group<L>& G, int itmax, int shift,
-                              const float2* __restrict__ est) {
+                              const float2* __restrict__ est, int scaled_min_n) {
   const int n = V.T.n;
-  const int status = schur_qr<L>(V, G, nullptr, nullptr, 1.0, itmax, est);
+  const int status = (n >= scaled_min_n && n >= kScaledMinN) ? schur_qr_scaled<L>(V, G, nullptr, nullptr, 1.0, itmax, est)
+                                                            : schur_qr<L>(V, G, nullptr, nullptr, 1.0, itmax, est);
   const double unscale = shift != 0 ? pow2(shift) : 1.0;
   for (int i = G.rank; i < n; i += L) {
     const double2 d = *V.T.at(i, i);
@@ -102,7 +103,8 @@ __global__ void __launch_bounds__(128) zgeev_vectors_kernel(int n, int batch, co
                                                             double2* __restrict__ w, double2* __restrict__ VL,
                                                             double2* __restrict__ VR, double2* __restrict__ work,
                                                             char* __restrict__ flag, int itmax,
-                                                            const float2* __restrict__ est, int* __restrict__ state) {
+                                                            const float2* __restrict__ est, int* __restrict__ state,
+                                                            int scaled_min_n) {
   constexpr int TW = 32 / L;
   const int lane = threadIdx.x & 31;
   const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -125,7 +127,7 @@ __global__ void __launch_bounds__(128) zgeev_vectors_kernel(int n, int batch, co
   if (kPhase == kPhaseQR) {
     const int s = state[j];
     if (s == kStateDone) return;  // group-uniform
-    status = vectors_finish<L>(w + j * n, vl, vr, V, G, itmax, s, e);
+    status = vectors_finish<L>(w + j * n, vl, vr, V, G, itmax, s, e, scaled_min_n);
   } else {
     int shift;
     status = vectors_prepare<L>(A + j * nn, w + j * n, vl, vr, V, G, shift);
@@ -133,7 +135,7 @@ __global__ void __launch_bounds__(128) zgeev_vectors_kernel(int n, int batch, co
       if (G.rank == 0) state[j] = status == kPrepared ? shift : kStateDone;
       if (status == kPrepared) return;
     } else if (status == kPrepared) {
-      status = vectors_finish<L>(w + j * n, vl, vr, V, G, itmax, shift, e);
+      status = vectors_finish<L>(w + j * n, vl, vr, V, G, itmax, shift, e, scaled_min_n);
     }
   }
   if (G.rank == 0) flag[j] = (char)status;
@@ -146,14 +148,15 @@ size_t vectors_workspace_bytes(int n, int batch) {
 template <int kPhase>
 static cudaError_t launch_vectors_phase(int lanes, unsigned blocks, int threads, cudaStream_t stream, int n,
                                         int batch, const double2* A, double2* w, double2* VL, double2* VR,
-                                        double2* work, char* flag, int itmax, const float2* est, int* state) {
+                                        double2* work, char* flag, int itmax, const float2* est, int* state,
+                                        int scaled_min_n) {
   const auto launch = [&](auto k) -> cudaError_t {
     if (kPhase != kPhaseAll) {  // shared memory for the estimator running beside
       const cudaError_t err =
           cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
       if (err != cudaSuccess) return err;
     }
-    k<<<blocks, threads, 0, stream>>>(n, batch, A, w, VL, VR, work, flag, itmax, est, state);
+    k<<<blocks, threads, 0, stream>>>(n, batch, A, w, VL, VR, work, flag, itmax, est, state, scaled_min_n);
     return cudaGetLastError();
   };
   switch (lanes) {
@@ -170,7 +173,8 @@ static cudaError_t launch_vectors_phase(int lanes, unsigned blocks, int threads,
 // after the backward-sized workspace. With fj the estimator runs on fj->aux
 // beside the first half (stage, Hessenberg, Q); without, first on `stream`.
 cudaError_t launch_vectors(int lanes, int n, int batch, const double2* A, double2* w, double2* VL, double2* VR,
-                           double2* work, char* flag, int itmax, cudaStream_t stream, bool hints, const ForkJoin* fj) {
+                           double2* work, char* flag, int itmax, cudaStream_t stream, bool hints, const ForkJoin* fj,
+                           int scaled_min_n) {
   const int tw = 32 / lanes;
   const long long warps = ((long long)batch + tw - 1) / tw;
   const int threads = 32;  // one-warp blocks spread a resident batch evenly over the SMs
@@ -178,7 +182,7 @@ cudaError_t launch_vectors(int lanes, int n, int batch, const double2* A, double
   if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
   if (!hints)
     return launch_vectors_phase<kPhaseAll>(lanes, (unsigned)blocks, threads, stream, n, batch, A, w, VL, VR, work,
-                                           flag, itmax, nullptr, nullptr);
+                                           flag, itmax, nullptr, nullptr, scaled_min_n);
   float2* est = reinterpret_cast<float2*>(reinterpret_cast<char*>(work) + backward_workspace_bytes(n, batch));
   int* state = reinterpret_cast<int*>(est + (size_t)n * batch);
   const ContigBatch src{A, nullptr, n};
@@ -186,7 +190,7 @@ cudaError_t launch_vectors(int lanes, int n, int batch, const double2* A, double
   if (fj == nullptr || fj->aux == nullptr) {
     if ((err = launch_estimates(n, batch, src, est, stream)) != cudaSuccess) return err;
     return launch_vectors_phase<kPhaseAll>(lanes, (unsigned)blocks, threads, stream, n, batch, A, w, VL, VR, work,
-                                           flag, itmax, est, nullptr);
+                                           flag, itmax, est, nullptr, scaled_min_n);
   }
   std::lock_guard<std::mutex> lock(*fj->mu);
   if ((err = cudaEventRecord(fj->fork, stream)) != cudaSuccess) return err;
@@ -194,11 +198,11 @@ cudaError_t launch_vectors(int lanes, int n, int batch, const double2* A, double
   if ((err = launch_estimates(n, batch, src, est, fj->aux)) != cudaSuccess) return err;
   if ((err = cudaEventRecord(fj->join, fj->aux)) != cudaSuccess) return err;
   if ((err = launch_vectors_phase<kPhasePrepare>(lanes, (unsigned)blocks, threads, stream, n, batch, A, w, VL, VR,
-                                                 work, flag, itmax, nullptr, state)) != cudaSuccess)
+                                                 work, flag, itmax, nullptr, state, scaled_min_n)) != cudaSuccess)
     return err;
   if ((err = cudaStreamWaitEvent(stream, fj->join, 0)) != cudaSuccess) return err;
   return launch_vectors_phase<kPhaseQR>(lanes, (unsigned)blocks, threads, stream, n, batch, A, w, VL, VR, work, flag,
-                                        itmax, est, state);
+                                        itmax, est, state, scaled_min_n);
 }
 
 }  // namespace tzg
