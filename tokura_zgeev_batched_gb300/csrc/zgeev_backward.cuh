@@ -295,7 +295,8 @@ __device__ int schur_qr_scaled(const BwdViews& V, const Group<L>& G, const doubl
       const int tcount = strided_count(G.rank, qend, L);
       const int qcount = strided_count(G.rank, n - 1, L);
       if (g.c != 0.0) {
-        const double rl = 1.0 / (g.c * u0 * u1);
+        double rl, rr2;
+        rotation_reciprocals(g.c, u0, u1, v0, v1, rl, rr2);
         const double2 alpha = cscale(g.s, u1 * u1 * rl);
         const double2 beta = make_double2(-g.s.x * (u0 * u0 * rl), g.s.y * (u0 * u0 * rl));
         if (j > lo && G.rank == 0) {
@@ -308,7 +309,6 @@ __device__ int schur_qr_scaled(const BwdViews& V, const Group<L>& G, const doubl
         u0 *= g.c;
         u1 *= g.c;
         G.sync();
-        const double rr2 = 1.0 / (g.c * v0 * v1);
         const double2 gamma = make_double2(g.s.x * (v1 * v1 * rr2), -g.s.y * (v1 * v1 * rr2));
         const double2 delta = cscale(g.s, -(v0 * v0 * rr2));
         TZG_DBG_RUN(T, G.rank, j, L, 0, tcount, 0, 1);

@@ -48,6 +48,23 @@ __device__ __forceinline__ double2* scale_slot(const MatView& M, int k) {
   return k <= M.n - 4 ? M.at(k + 3, 0) : M.at(k - M.n + 7, 1);
 }
 
+// 1/(c u0 u1) and 1/(c v0 v1) from one reciprocal of their product when it
+// stays normal (c and the factors can each be as small as ~1e-145 and 2^-60),
+// else from two.
+__device__ __forceinline__ void rotation_reciprocals(double c, double u0, double u1, double v0, double v1, double& rl,
+                                                     double& rr) {
+  const double pl = c * u0 * u1, pr = c * v0 * v1;
+  const double prod = pl * pr;
+  if (prod > 1e-290) {
+    const double inv = 1.0 / prod;
+    rl = inv * pr;
+    rr = inv * pl;
+  } else {
+    rl = 1.0 / pl;
+    rr = 1.0 / pr;
+  }
+}
+
 // a + f * b (complex multiply-add, 4 FP64 instructions).
 __device__ __forceinline__ double2 cmadd(double2 a, double2 f, double2 b) {
   return make_double2(fma(f.x, b.x, fma(-f.y, b.y, a.x)), fma(f.x, b.y, fma(f.y, b.x, a.y)));
@@ -202,7 +219,8 @@ __device__ int qr_eigenvalues_scaled(const MatView& M, const Group<L>& G, Out* _
       const int q0 = lo + G.rank;
       if (g.c != 0.0) {
         // Left: rows (j, j+1) over columns j .. i (and j-1, whose row j+1 entry is annihilated).
-        const double rl = 1.0 / (g.c * u0 * u1);
+        double rl, rr2;
+        rotation_reciprocals(g.c, u0, u1, v0, v1, rl, rr2);
         const double2 alpha = cscale(g.s, u1 * u1 * rl);
         const double2 beta = make_double2(-g.s.x * (u0 * u0 * rl), g.s.y * (u0 * u0 * rl));
         if (j > lo && G.rank == 0) {
@@ -217,7 +235,6 @@ __device__ int qr_eigenvalues_scaled(const MatView& M, const Group<L>& G, Out* _
         G.sync();
         // Right: columns (j, j+1) over rows lo .. min(j+1, i); row j+2 gets the new bulge
         // K(j+2, j) = gamma K(j+2, j+1) (its column-j entry is zero), K(j+2, j+1) unchanged.
-        const double rr2 = 1.0 / (g.c * v0 * v1);
         const double2 gamma = make_double2(g.s.x * (v1 * v1 * rr2), -g.s.y * (v1 * v1 * rr2));
         const double2 delta = cscale(g.s, -(v0 * v0 * rr2));
         TZG_DBG_RUN(M, q0, j, L, 0, strided_count(q0, qend, L), 0, 1);
