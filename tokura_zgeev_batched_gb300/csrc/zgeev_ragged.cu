@@ -128,19 +128,6 @@ __global__ void __launch_bounds__(1024) ragged_scan_kernel(int batch, const int*
   }
 }
 
-// Lane width of a ragged launch when the caller did not fix one: the smallest
-// L such that a tile of 32/L order-64 matrices (the worst case the host can
-// assume) stays below a third of the average work of an SM sub-partition,
-// estimated from batch_count and the mean order sqrt(total_elements/batch).
-int ragged_auto_lanes(int sms, int batch, long long total_elements) {
-  const double mean_n = std::sqrt((double)total_elements / (double)batch);
-  const auto work = [](double n) { return 25.0 * n * n * n + 400.0 * n * n; };
-  const double per_smsp = (double)batch * work(mean_n) / (32.0 * 4.0 * (double)(sms > 0 ? sms : 1));
-  int lanes = 1;
-  while (lanes < 8 && work(64.0) / lanes > per_smsp / 3.0) lanes *= 2;
-  return lanes;
-}
-
 // Device-side planning shared by the forward and backward ragged solvers.
 static cudaError_t ragged_prepare(int lanes, int sms, int batch, const int* n, const long long* offsets,
                                   const long long* eig_offsets, long long total_elements, const RaggedLayout& lay,
@@ -174,8 +161,8 @@ cudaError_t launch_ragged(int lanes, int sms, int batch, const int* n, const lon
                           int hint_min_n, const ForkJoin* fj, int scaled_min_n) {
   // Shift hints for the matrices of order >= hint_min_n (0: none).
   const bool hints = hint_min_n > 0 && hint_min_n <= kMaxN;
-  if (lanes == 0) lanes = ragged_auto_lanes(sms, batch, total_elements);
-  if (!(lanes == 1 || lanes == 2 || lanes == 4 || lanes == 8)) return cudaErrorInvalidValue;
+  // lanes == 0: each size bin gets its own lane width from the planner (ragged_plan_kernel).
+  if (!(lanes == 0 || lanes == 1 || lanes == 2 || lanes == 4 || lanes == 8)) return cudaErrorInvalidValue;
   const RaggedLayout lay = ragged_layout(batch, total_elements);
   char* w = static_cast<char*>(work);
   double2* stage = reinterpret_cast<double2*>(w + lay.stage_off);
@@ -197,10 +184,8 @@ cudaError_t launch_ragged(int lanes, int sms, int batch, const int* n, const lon
   err = ragged_prepare(lanes, sms, batch, n, offsets, eig_offsets, total_elements, lay, work, flag, stream, &plan,
                        &sorted, &eo);
   if (err != cudaSuccess) return err;
-  // scaled_min_n is per lane: orders >= lanes * scaled_min_n (at least 7; 65 or more: never)
-  const int scaled_from = scaled_min_n > 64 ? 65 : max(7, min(65, scaled_min_n * lanes));
   const RaggedArgs args{offsets, eo, A, eig, nullptr, nullptr, nullptr, stage, total_elements, flag, sorted,
-                        itmax_override, balance, est, state, hint_min_n, scaled_from};
+                        itmax_override, balance, est, state, hint_min_n, scaled_min_n};
   if (split) return ragged_launch_phases(lanes, sms, plan, args, balance != 0, stream, *fj);
   if (balance != 0) return launch_ragged_kernel<false, true, kPhaseAll>(lanes, sms, plan, args, stream);
   return launch_ragged_kernel<false, false, kPhaseAll>(lanes, sms, plan, args, stream);
@@ -210,8 +195,7 @@ cudaError_t launch_ragged_backward(int lanes, int sms, int batch, const int* n, 
                                    const long long* eig_offsets, long long total_elements, const double2* A,
                                    const double2* lam, const double2* gbar, double2* gA, void* work, char* flag,
                                    int itmax_override, cudaStream_t stream, int scaled_min_n) {
-  if (lanes == 0) lanes = ragged_auto_lanes(sms, batch, total_elements);
-  if (!(lanes == 1 || lanes == 2 || lanes == 4 || lanes == 8)) return cudaErrorInvalidValue;
+  if (!(lanes == 0 || lanes == 1 || lanes == 2 || lanes == 4 || lanes == 8)) return cudaErrorInvalidValue;
   const RaggedLayout lay = ragged_layout(batch, total_elements, 4);
   double2* stage = reinterpret_cast<double2*>(static_cast<char*>(work) + lay.stage_off);
   RaggedPlan* plan;
@@ -220,9 +204,8 @@ cudaError_t launch_ragged_backward(int lanes, int sms, int batch, const int* n, 
   cudaError_t err = ragged_prepare(lanes, sms, batch, n, offsets, eig_offsets, total_elements, lay, work, flag,
                                    stream, &plan, &sorted, &eo);
   if (err != cudaSuccess) return err;
-  const int scaled_from = scaled_min_n > 64 ? 65 : max(7, min(65, scaled_min_n * lanes));
   const RaggedArgs args{offsets, eo, A, nullptr, lam, gbar, gA, stage, total_elements, flag, sorted, itmax_override,
-                        0, nullptr, nullptr, 0, scaled_from};
+                        0, nullptr, nullptr, 0, scaled_min_n};
   return launch_ragged_kernel<true, false, kPhaseAll>(lanes, sms, plan, args, stream);
 }
 

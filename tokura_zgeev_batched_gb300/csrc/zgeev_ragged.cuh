@@ -89,7 +89,7 @@ struct RaggedArgs {
   const float2* est;     // forward: FP32 shift hints, kMaxN per matrix (or null)
   int* state;            // forward, split solve: pre-scaling exponent or kStateDone per matrix
   int est_min_n;         // forward: orders from which est holds hints
-  int scaled_min_n = 65;  // forward: orders from which the QR uses scaled rotations (zgeev_scaled_qr.cuh)
+  int scaled_min_n = 65;  // QR with scaled rotations from order max(7, lanes * scaled_min_n); > 64: never
 };
 
 // Tile scheduling. Tiles are numbered in descending-work order; SM s owns
@@ -116,17 +116,61 @@ __device__ __forceinline__ int ragged_next_tile(int* queue, int queues, int num_
   return -1;
 }
 
-// Persistent solver with L lanes per matrix: takes tiles until all shares are
-// used up and solves (kBackward = false) or differentiates (true) each one;
-// kBalance (forward only) balances each matrix first with a.balance. The
-// forward runs whole (kPhaseAll) or split: kPhasePrepare stages and reduces
-// every matrix and records its state, kPhaseQR finishes it with the hints.
-// One instantiation per lane width, so each has its own register budget.
+// Solves (kBackward = false) or differentiates (true) the matrices of tile t
+// of `bin` with L lanes per matrix; kBalance (forward only) balances each
+// matrix first with a.balance. The forward runs whole (kPhaseAll) or split:
+// kPhasePrepare stages and reduces every matrix and records its state,
+// kPhaseQR finishes it with the hints.
 template <int L, bool kBackward, bool kBalance, int kPhase>
-__global__ void __launch_bounds__(128) zgeev_ragged_kernel(RaggedPlan* plan, RaggedArgs a, int queues) {
+__device__ __forceinline__ void ragged_tile(const RaggedBin& bin, int t, const RaggedArgs& a, int lane) {
   constexpr int TW = 32 / L;
-  const int lane = threadIdx.x & 31;
   const int slot = lane / L;
+  const int u = t - bin.tile_start;
+  const int tw = min(TW, bin.count - u * TW);
+  if (slot >= tw) return;  // whole lane groups leave together
+  const Group<L> G;
+  const int nb = bin.n;
+  const int j = a.sorted[bin.first + u * TW + slot];
+  const long long nn = (long long)nb * nb;
+  double2* base = a.stage + bin.stage + (long long)u * TW * nn + slot;
+  const int itmax = a.itmax_override > 0 ? a.itmax_override : default_itmax(nb);
+  const float2* est = a.est != nullptr && nb >= a.est_min_n ? a.est + (long long)j * kMaxN : nullptr;
+  // scaled rotations from order max(7, L * scaled_min_n) (a.scaled_min_n > 64: never)
+  const bool scaled = a.scaled_min_n <= kMaxN && nb >= kScaledMinN && nb >= L * a.scaled_min_n;
+  int status = kPrepared;  // kPrepared: no flag to write yet
+  if (kBackward) {
+    BwdViews V{MatView{base, nb, tw}, MatView{base + a.region, nb, tw}, MatView{base + 2 * a.region, nb, tw},
+               base + 3 * a.region, tw};
+    status = backward_matrix<L>(a.A + a.offsets[j], a.lam + a.eoff[j], a.gbar + a.eoff[j], a.gA + a.offsets[j], V,
+                                G, itmax, scaled ? nb : kMaxN + 1);
+  } else if (kPhase == kPhaseAll) {
+    int shift;
+    const MatView M{base, nb, tw};
+    status = prepare_matrix<L, kBalance>(SrcContig{a.A + a.offsets[j]}, M, G, a.eig + a.eoff[j], a.balance, shift);
+    if (status == kPrepared)
+      status = scaled ? qr_eigenvalues_scaled<L>(M, G, a.eig + a.eoff[j], shift, itmax, est)
+                      : qr_eigenvalues<L>(M, G, a.eig + a.eoff[j], shift, itmax, est);
+  } else if (kPhase == kPhasePrepare) {
+    int shift;
+    status = prepare_matrix<L, kBalance>(SrcContig{a.A + a.offsets[j]}, MatView{base, nb, tw}, G, a.eig + a.eoff[j],
+                                         a.balance, shift);
+    if (G.rank == 0) a.state[j] = status != kPrepared ? kStateDone : shift;
+  } else {
+    const int s = a.state[j];
+    if (s != kStateDone)
+      status = scaled ? qr_eigenvalues_scaled<L>(MatView{base, nb, tw}, G, a.eig + a.eoff[j], s, itmax, est)
+                      : qr_eigenvalues<L>(MatView{base, nb, tw}, G, a.eig + a.eoff[j], s, itmax, est);
+  }
+  if (G.rank == 0 && status != kPrepared) a.flag[j] = (char)status;
+}
+
+// Persistent solver: takes tiles until all shares are used up. kL = 1, 2, 4 or
+// 8 fixes the lanes per matrix for every tile (one instantiation per width, so
+// each has its own register budget); kL = 0 takes each tile's width from its
+// bin (the planner's per-bin choice; one kernel holds all four variants).
+template <int kL, bool kBackward, bool kBalance, int kPhase>
+__global__ void __launch_bounds__(128) zgeev_ragged_kernel(RaggedPlan* plan, RaggedArgs a, int queues) {
+  const int lane = threadIdx.x & 31;
   const int num_tiles = plan->num_tiles;
   int* queue = kPhase == kPhaseQR ? plan->queue_qr : plan->queue;
   int q = (int)(sm_id() % (unsigned)queues);
@@ -136,44 +180,15 @@ __global__ void __launch_bounds__(128) zgeev_ragged_kernel(RaggedPlan* plan, Rag
     t = __shfl_sync(0xffffffffu, t, 0);
     if (t < 0) break;
     const RaggedBin& bin = ragged_bin_of(plan, t);
-    const int u = t - bin.tile_start;
-    const int tw = min(TW, bin.count - u * TW);
-    if (slot < tw) {
-      const Group<L> G;
-      const int nb = bin.n;
-      const int j = a.sorted[bin.first + u * TW + slot];
-      const long long nn = (long long)nb * nb;
-      double2* base = a.stage + bin.stage + (long long)u * TW * nn + slot;
-      const int itmax = a.itmax_override > 0 ? a.itmax_override : default_itmax(nb);
-      const float2* est = a.est != nullptr && nb >= a.est_min_n ? a.est + (long long)j * kMaxN : nullptr;
-      int status = kPrepared;  // kPrepared: no flag to write yet
-      if (kBackward) {
-        BwdViews V{MatView{base, nb, tw}, MatView{base + a.region, nb, tw}, MatView{base + 2 * a.region, nb, tw},
-                   base + 3 * a.region, tw};
-        status = backward_matrix<L>(a.A + a.offsets[j], a.lam + a.eoff[j], a.gbar + a.eoff[j],
-                                    a.gA + a.offsets[j], V, G, itmax, a.scaled_min_n);
-      } else if (kPhase == kPhaseAll) {
-        int shift;
-        const MatView M{base, nb, tw};
-        status = prepare_matrix<L, kBalance>(SrcContig{a.A + a.offsets[j]}, M, G, a.eig + a.eoff[j], a.balance,
-                                             shift);
-        if (status == kPrepared)
-          status = (nb >= a.scaled_min_n && nb >= kScaledMinN)
-                       ? qr_eigenvalues_scaled<L>(M, G, a.eig + a.eoff[j], shift, itmax, est)
-                       : qr_eigenvalues<L>(M, G, a.eig + a.eoff[j], shift, itmax, est);
-      } else if (kPhase == kPhasePrepare) {
-        int shift;
-        status = prepare_matrix<L, kBalance>(SrcContig{a.A + a.offsets[j]}, MatView{base, nb, tw}, G,
-                                             a.eig + a.eoff[j], a.balance, shift);
-        if (G.rank == 0) a.state[j] = status != kPrepared ? kStateDone : shift;
-      } else {
-        const int s = a.state[j];
-        if (s != kStateDone)
-          status = (nb >= a.scaled_min_n && nb >= kScaledMinN)
-                       ? qr_eigenvalues_scaled<L>(MatView{base, nb, tw}, G, a.eig + a.eoff[j], s, itmax, est)
-                       : qr_eigenvalues<L>(MatView{base, nb, tw}, G, a.eig + a.eoff[j], s, itmax, est);
+    if (kL != 0) {
+      ragged_tile<kL == 0 ? 1 : kL, kBackward, kBalance, kPhase>(bin, t, a, lane);
+    } else {
+      switch (bin.lanes) {  // warp-uniform
+        case 1: ragged_tile<1, kBackward, kBalance, kPhase>(bin, t, a, lane); break;
+        case 2: ragged_tile<2, kBackward, kBalance, kPhase>(bin, t, a, lane); break;
+        case 4: ragged_tile<4, kBackward, kBalance, kPhase>(bin, t, a, lane); break;
+        default: ragged_tile<8, kBackward, kBalance, kPhase>(bin, t, a, lane); break;
       }
-      if (G.rank == 0 && status != kPrepared) a.flag[j] = (char)status;
     }
     __syncwarp();
   }
@@ -203,6 +218,7 @@ template <bool kBackward, bool kBalance, int kPhase>
 inline cudaError_t launch_ragged_kernel(int lanes, int sms, RaggedPlan* plan, const RaggedArgs& args,
                                         cudaStream_t stream) {
   switch (lanes) {
+    case 0: return launch_ragged_l<0, kBackward, kBalance, kPhase>(sms, plan, args, stream);
     case 1: return launch_ragged_l<1, kBackward, kBalance, kPhase>(sms, plan, args, stream);
     case 2: return launch_ragged_l<2, kBackward, kBalance, kPhase>(sms, plan, args, stream);
     case 4: return launch_ragged_l<4, kBackward, kBalance, kPhase>(sms, plan, args, stream);
