@@ -961,13 +961,16 @@ def run_ours(args):
 
     kern_avg = statistics.mean(kern_ms)
     achieved = flops_per_matrix(N) * BATCH / (kern_avg * 1e-3)
+    # DRAM bytes of one call: the per-matrix traffic of an ncu capture (profiles/traffic.json)
+    # times this batch; the capture's conditions and the scaling are stated there.
     prof = read_profile_traffic()
-    traffic = None
-    if prof and prof.get("n") == N:
-        traffic = prof.get("dram_bytes_per_launch")
+    traffic = traffic_note = None
+    if prof and prof.get("n") == N and prof.get("dram_bytes_per_matrix"):
+        traffic = prof["dram_bytes_per_matrix"] * BATCH
+        traffic_note = prof.get("scaling")
     roofline = {
         "bound": "fp64", "achieved": achieved / 1e12, "peak": peak / 1e12, "unit": "TFLOP/s",
-        "frac": achieved / peak, "traffic": traffic,
+        "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_note,
         "peak_source": "FP64 FMA-loop probe run in this process (MEASURED_PEAKS.json has no FP64 figure)",
         "algorithmic": f"40*n^3 flops and 16*n^2+16*n+1 bytes per matrix x {BATCH} matrices per launch",
         "kernel_ms_avg": kern_avg,
@@ -1136,8 +1139,10 @@ def run_ours(args):
             "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "c128 (f64)", "data": "synthetic",
             "config": {"workload": f"plain zgeev eigenvalues (tokura_zgeev_batched_gpu), n={N}, {BATCH} complex "
-                                   f"Gaussian matrices per GPU (4 GiB), seed {SEED}",
-                       "n": N, "global_batch": ws * BATCH, "l2": "inputs (4 GiB) larger than L2",
+                                   f"Gaussian matrices per GPU ({16 * N * N * BATCH / 2 ** 30:.2f} GiB), seed {SEED}",
+                       "n": N, "global_batch": ws * BATCH,
+                       "l2": f"inputs ({16 * N * N * BATCH / 2 ** 20:.0f} MiB) "
+                             f"{'larger' if 16 * N * N * BATCH > 129 * 2 ** 20 else 'smaller'} than L2 (129 MB)",
                        "lanes_per_matrix": h.plain_config(N, BATCH)[0],
                        "shift_hints": "FP32 estimator on a second stream beside the FP64 Hessenberg kernel, then "
                                       "the FP64 QR kernel" if N >= SHIFT_HINT_MIN_N else "off (n < 12)"},
