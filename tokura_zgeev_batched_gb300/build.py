@@ -39,6 +39,7 @@ SOURCES = [
     "dgeev_batched.cu",
     "zgeev_ragged.cu",
     "zgeev_ragged_split.cu",
+    "zgeev_ragged_bwd.cu",
     "tokura_tuner.cu",
     "zgeev_backward.cu",
     "zgeev_vectors.cu",

@@ -227,6 +227,12 @@ inline cudaError_t launch_ragged_kernel(int lanes, int sms, RaggedPlan* plan, co
   }
 }
 
+// Device-side planning shared by the forward and backward solvers (zgeev_ragged.cu).
+cudaError_t ragged_prepare(int lanes, int sms, int batch, const int* n, const long long* offsets,
+                           const long long* eig_offsets, long long total_elements, const RaggedLayout& lay,
+                           void* work, char* flag, cudaStream_t stream, RaggedPlan** plan_out, int** sorted_out,
+                           const long long** eoff_out);
+
 // Defined in zgeev_ragged_split.cu (the hinted, two-phase forward).
 // Estimator for every valid matrix of order >= min_n, on `stream`.
 cudaError_t launch_ragged_estimates(int sms, int batch, const int* n, const long long* offsets, long long total,
