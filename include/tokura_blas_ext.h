@@ -208,7 +208,7 @@ TOKURA_API int tokuraSetHostLinkRate(tokurablas_t* handle, double gbs);
 
 /* Host-buffer variant of tokura_zgeev_batched_gpu: A, eigenvalues and flag are
  * HOST pointers (layouts as the device call). The batch is cut into chunks of
- * chunk_matrices (0 = automatic: 4 equal chunks, or growing chunks from 1/16
+ * chunk_matrices (0 = automatic: 2 equal chunks, or growing chunks from 1/16
  * of the batch when the previous call on the handle saw a host-to-device rate
  * below 100 GB/s) issued round-robin on the handle's own streams, copies in
  * chunk order, so host-device copies overlap the solves; returns when the results

@@ -46,7 +46,7 @@ def test_host_entry_argument_codes(cuda):
 @pytest.mark.parametrize("batch", [3000, 10000, 40000])
 def test_host_entry_default_plans_bitwise_equal_device_call(cuda, batch, link_gbs):
     """Both default chunk plans (slow link: 1/16, 1/16, 1/8, 1/4, 1/2 of the
-    batch; fast link: 4 equal chunks; each at least 1,024 matrices) cut the
+    batch; fast link: 2 equal chunks; each at least 1,024 matrices) cut the
     batch differently from the device call, but every matrix is solved by the
     same arithmetic: bitwise the same results. 0 = the measured rate: the
     second call plans with the rate the first one saw."""

@@ -90,12 +90,13 @@ extern "C" TOKURA_API int tokura_zgeev_batched_host(tokurablas_t* handle, int n,
   // equal chunks of that size, round-robin over up to 16 streams. Otherwise
   // by the host-to-device rate the previous call saw (or the caller set with
   // tokuraSetHostLinkRate):
-  //  * fast link (>= kFastLinkGBs; or the first call): 4 equal chunks (at
+  //  * fast link (>= kFastLinkGBs; or the first call): 2 equal chunks (at
   //    least 1,024 matrices each). All copies land within a few percent of the
-  //    solve time, and fewer, larger chunks leave the shortest tail (65,536
-  //    64x64 matrices over a 211 GB/s link: 693 ms with 4 chunks, 721 ms with
-  //    the growing plan, 726 ms with 8 chunks, against 676 ms for the solve
-  //    alone).
+  //    solve time, and fewer, larger chunks leave the shortest tail: 65,536
+  //    64x64 matrices over a 211 GB/s link took 597-599 ms with 2 chunks,
+  //    615 ms with 1, 625-642 ms with 4, 699 ms with 8, against 592 ms for the
+  //    solve alone (the second chunk's copy overlaps the first chunk's solve,
+  //    and the two solves together fill the GPU).
   //  * slow link: growing chunks of 1/16, 1/16, 1/8, 1/4, 1/2 of the batch (at
   //    least 1,024 matrices each): the first solve starts after a small copy,
   //    and while the largest chunk is still arriving the earlier ones keep the
@@ -108,7 +109,7 @@ extern "C" TOKURA_API int tokura_zgeev_batched_host(tokurablas_t* handle, int n,
   } else if (const double rate = P.link_gbs_fixed > 0.0 ? P.link_gbs_fixed : P.link_gbs;
              rate == 0.0 || rate >= kFastLinkGBs) {
     int parts = (batch_count + 1023) / 1024;
-    if (parts > 4) parts = 4;
+    if (parts > 2) parts = 2;
     const int c = (int)(((long long)batch_count + parts - 1) / parts);
     for (long long first = 0; first < batch_count; first += c)
       sizes.push_back((int)(batch_count - first < c ? batch_count - first : c));
