@@ -207,7 +207,13 @@ def test_reference_header_constants_and_enums(tmp_path):
         assert r.returncode == 0, r.stderr
 
 
-REFERENCE_DRIVER = "/root/reference/stream_test/main.cu"
+def _reference_driver() -> str:
+    from oracle import ref_gpu
+
+    return os.path.join(ref_gpu.reference_root(), "stream_test", "main.cu")
+
+
+REFERENCE_DRIVER = _reference_driver()
 
 
 @pytest.mark.skipif(not os.path.exists(REFERENCE_DRIVER), reason="the reference's sources are not mounted here")
