@@ -372,9 +372,9 @@ def measure_real(h, dev, stream, peak, n: int = 64, batch: int = 65536, cpu_seco
             "cpu_lapack_dgeev": {"matrices_per_s": cpu_count / t, "threads": threads, "sample": cpu_count}}
 
 
-def measure_vectors(h, dev, stream, n: int = 64, batch: int = 16384, cpu_seconds: float = 2.0) -> dict:
-    """Eigenvalues with left and right eigenvectors (tokura_zgeev_vectors_batched_gpu) on complex
-    Gaussian matrices: matrices/s (raw C-ABI call on device buffers), residuals
+def measure_vectors(h, dev, stream, n: int = 64, batch: int = 65536, cpu_seconds: float = 2.0) -> dict:
+    """Eigenvalues with left and right eigenvectors (tokura_zgeev_vectors_batched_gpu) on 65,536 complex
+    Gaussian 64x64 matrices (the eigenvalue workload's batch; about 13 GiB of A, VL and VR): matrices/s (raw C-ABI call on device buffers), residuals
     ||A VR - VR diag(w)|| / ||A|| and ||VL^H A - diag(w) VL^H|| / ||A|| on a sample, and LAPACK
     zgeev('V','V') over the host cores on a bounded sample for comparison."""
     import torch
@@ -1174,7 +1174,7 @@ def run_only(args):
     elif args.only == "real":
         out = measure_real(h, dev, stream, peak, n=args.n, batch=args.batch or 65536, cpu_seconds=0.5)
     elif args.only == "vectors":
-        out = measure_vectors(h, dev, stream, n=args.n, batch=args.batch or 16384, cpu_seconds=0.5)
+        out = measure_vectors(h, dev, stream, n=args.n, batch=args.batch or 65536, cpu_seconds=0.5)
     elif args.only == "config1":
         def call(n, batch, A, eig, flag, work):
             st = api.tokura_zgeev_batched_gpu(h, n, batch, A.data_ptr(), eig.data_ptr(), work.data_ptr(),
