@@ -284,16 +284,15 @@ TOKURA_API int tokuraSetRealConfig(tokurablas_t* handle, int n, int lanes_per_ma
 /* Same computation and outputs as tokura_zgeev_batched_gpu, but it allocates
  * nothing and takes no workspace: it has no counterpart in the reference.
  * It is for callers that cannot allocate device memory when they need the
- * eigenvalues — e.g. code running during a global-mode stream capture, where
- * cudaMalloc is refused, or plugins whose host application owns all device
+ * eigenvalues — e.g. plugins whose host application owns all device
  * memory. The staging area is a 32 MiB static device array in the library
  * (held by every GPU that loads it until exit), so 16*n*n*batch_count must be
  * <= tokura_zgeev_noalloc_max_bytes(): at most 512 matrices of order 64,
  * 2048 of order 32 (the shift hints of tokuraSetShiftHints are used when
  * their (8*n + 4)*batch_count bytes of estimates and phase state also fit:
  * up to 508 matrices of order 64, 2016 of order 32). The first call on a
- * device looks up that array's device address, so make it before any stream
- * capture starts; the address is kept for the life of the process, so calls
+ * device looks up that array's device address (a host-side query); the
+ * address is kept for the life of the process, so calls
  * after a cudaDeviceReset of that device are not supported. The handle's
  * device must be the current device (else 1). All calls share the
  * array: calls that overlap on the GPU race and must be ordered by the

@@ -1,8 +1,7 @@
 """The workspace-free entry point tokura_zgeev_batched_gpu_noalloc, through the C ABI.
 
 Some callers cannot allocate device memory when they need eigenvalues (for
-example during a global-mode stream capture, or inside a host application
-that owns all device memory); this entry point stages matrices in a static
+example inside a host application that owns all device memory); this entry point stages matrices in a static
 32 MiB device array instead of a caller workspace. Its results must match the
 regular entry point's on the same inputs, on consecutive calls that reuse the
 array. This file is collected last on purpose.

@@ -2,10 +2,9 @@
 // caller-provided workspace.
 //
 // Who needs it: callers that cannot allocate device memory at the moment they
-// need eigenvalues — for example code running while a stream is being captured
-// in cudaStreamCaptureModeGlobal (where cudaMalloc is refused), or a plugin
-// living inside a host application that owns the whole device-memory budget
-// and forbids out-of-band allocations. They still pass A, eigenvalues and flag.
+// need eigenvalues — for example a plugin living inside a host application
+// that owns the whole device-memory budget and forbids out-of-band
+// allocations. They still pass A, eigenvalues and flag.
 //
 // The kernel's staging area (the tile-interleaved copy of A) lives in a
 // file-scope __device__ array of kNoAllocScratchBytes (32 MiB), which every GPU
@@ -18,7 +17,7 @@
 // Host code must not hand the array's name to a kernel: on the host it is only
 // a stand-in symbol. The device address is obtained once per device, with that
 // device current, by cudaGetSymbolAddress on the first call made on that device
-// (so make that first call before any stream capture begins); the address is
+// (a host-side query); the address is
 // cached for the life of the process, so a cudaDeviceReset of that device
 // invalidates it and later calls are unsupported. All calls share
 // the array and it keeps the previous call's contents; the kernel overwrites
