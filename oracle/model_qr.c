@@ -17,6 +17,7 @@
  */
 #include <math.h>
 #include <stdlib.h>
+#include <string.h>
 
 typedef struct { double re, im; } zc;
 
@@ -32,13 +33,14 @@ static zc zdiv(zc a, zc b) {
   double d = zabs2(b);
   return z((a.re * b.re + a.im * b.im) / d, (a.im * b.re - a.re * b.im) / d);
 }
-static zc zsqrt(zc v) {
-  double m = hypot(v.re, v.im);
-  if (m == 0.0) return z(0.0, 0.0);
-  double t = sqrt(0.5 * (m + fabs(v.re)));
-  double h = v.im / (2.0 * t);
-  return v.re >= 0.0 ? z(t, h) : z(fabs(h), copysign(t, v.im));
+/* Unbiased exponent field of |v| (-1023 for zero and subnormals), as the GPU's
+ * dexp_field - 1023. */
+static int expo(double v) {
+  unsigned long long u;
+  memcpy(&u, &v, sizeof u);
+  return (int)((u >> 52) & 0x7ff) - 1023;
 }
+static int floor_half(int e) { return e >= 0 ? e / 2 : -((1 - e) / 2); }
 
 #define H(r, c) a[(size_t)(c) * n + (r)]
 
@@ -133,18 +135,31 @@ static int negligible(int n, const zc* a, int k, int lo, int hi, double smlnum, 
   return ba * (ab / s) <= fmax(smlnum, tol * (bb * (aa / s)));
 }
 
-/* Eigenvalue of [[a, b], [c, d]] nearer to d, in a scaled form. */
+/* Eigenvalue of [[a, b], [c, d]] nearer to d: d - bc / (x + sqrt(x^2 + bc)),
+ * x = (a - d)/2, root sign with Re(conj(x) y) >= 0, after scaling x and bc by
+ * the exact power of two 2^-k, k = max(exponent of |x|_1, floor(exponent of
+ * |bc|_1 / 2)); the principal root from u = (|z| + |Re z|)/2 (zgeev_device.cuh:
+ * wilkinson_shift, same operations). */
 static zc wilkinson(zc a, zc b, zc c, zc d) {
   zc bc = zmul(b, c);
   if (bc.re == 0.0 && bc.im == 0.0) return d;
   zc x = zscale(zsub(a, d), 0.5);
-  double sc = fmax(zabs1(x), sqrt(zabs1(bc)));
-  zc xs = zscale(x, 1.0 / sc), bcs = zscale(bc, 1.0 / (sc * sc));
-  zc y = zsqrt(zadd(zmul(xs, xs), bcs));
+  int ex = expo(zabs1(x)), eb = floor_half(expo(zabs1(bc)));
+  int k = ex > eb ? ex : eb;
+  double is = ldexp(1.0, -k);
+  zc xs = zscale(x, is), bcs = zscale(zscale(bc, is), is);
+  zc zz = zadd(zmul(xs, xs), bcs);
+  double u = 0.5 * (sqrt(zabs2(zz)) + fabs(zz.re));
+  zc y = z(0.0, 0.0);
+  if (u > 0.0) {
+    double r = 1.0 / sqrt(u), t = u * r, h = 0.5 * zz.im * r;
+    y = zz.re >= 0.0 ? z(t, h) : z(fabs(h), copysign(t, zz.im));
+  }
   if (xs.re * y.re + xs.im * y.im < 0.0) y = z(-y.re, -y.im);
   zc den = zadd(xs, y);
-  if (den.re == 0.0 && den.im == 0.0) return d;
-  return zsub(d, zscale(zdiv(bcs, den), sc));
+  double f = ldexp(1.0, k) / zabs2(den);
+  zc num = zmul(bcs, zconj(den));
+  return z(d.re - num.re * f, d.im - num.im * f);
 }
 
 /* Rotation [c s; -conj(s) c] (c real) taking (x, y) to (r, 0). */

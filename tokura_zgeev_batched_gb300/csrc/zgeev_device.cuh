@@ -42,31 +42,6 @@ __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
 }
 __device__ __forceinline__ double2 cscale(double2 a, double s) { return make_double2(a.x * s, a.y * s); }
 
-// Robust complex division p / q (Smith's method).
-__device__ __forceinline__ double2 cdiv(double2 p, double2 q) {
-  if (fabs(q.x) >= fabs(q.y)) {
-    if (q.x == 0.0) return make_double2(p.x / q.x, p.y / q.x);  // q == 0: inf/nan as IEEE says
-    double r = q.y / q.x;
-    double d = 1.0 / fma(q.y, r, q.x);
-    return make_double2(fma(p.y, r, p.x) * d, fma(-p.x, r, p.y) * d);
-  } else {
-    double r = q.x / q.y;
-    double d = 1.0 / fma(q.x, r, q.y);
-    return make_double2(fma(p.x, r, p.y) * d, fma(p.y, r, -p.x) * d);
-  }
-}
-
-// Principal complex square root, computed from |z| without overflow for the
-// magnitudes that occur here (entries are pre-scaled to ~1).
-__device__ __forceinline__ double2 csqrt_(double2 z) {
-  double m = hypot(z.x, z.y);
-  if (m == 0.0) return make_double2(0.0, 0.0);
-  double t = sqrt(0.5 * (m + fabs(z.x)));
-  double h = z.y / (2.0 * t);
-  if (z.x >= 0.0) return make_double2(t, h);
-  return make_double2(fabs(h), copysign(t, z.y));
-}
-
 // Biased exponent field of |x| (0 for zero/denormal, 2047 for inf/nan).
 __device__ __forceinline__ int dexp_field(double x) {
   return (__double2hiint(x) >> 20) & 0x7ff;
@@ -207,23 +182,40 @@ __device__ __forceinline__ int strided_count(int first, int last, int step) {
   return first <= last ? (last - first) / step + 1 : 0;
 }
 
-// Eigenvalue of [a b; c d] closest to d (Wilkinson shift), in a scaled,
-// cancellation-free form: d - bc / (x + sqrt(x^2 + bc)), x = (a - d)/2,
-// with the root's sign chosen so that |x + sqrt(.)| is maximal.
+// Eigenvalue of [a b; c d] closest to d (Wilkinson shift), in a
+// cancellation-free form: d - bc / (x + sqrt(x^2 + bc)), x = (a - d)/2, with
+// the root's sign chosen so that |x + sqrt(.)| is maximal (Re(conj(x) y) >= 0).
+// x and bc are first scaled by an exact power of two 2^-k, k taken from the
+// exponent fields, so that the larger of the scaled |x|_1, |bc|_1 lies in
+// [1, 4): squaring then neither overflows nor underflows, and with the sign
+// rule |x + y|^2 >= |x|^2 + |x^2 + bc| >= max(|x|^2, |bc|) >= 1/2, so the
+// quotient is bc * conj(x + y) times 2^k / |x + y|^2. One square root (of
+// |x^2 + bc|^2), one reciprocal square root (the principal root of
+// x^2 + bc) and one division in all.
 __device__ __forceinline__ double2 wilkinson_shift(double2 a, double2 b, double2 c, double2 d) {
   const double2 bc = cmul(b, c);
   if (bc.x == 0.0 && bc.y == 0.0) return d;
   const double2 x = make_double2(0.5 * (a.x - d.x), 0.5 * (a.y - d.y));
-  double sc = fmax(cabs1(x), sqrt(cabs1(bc)));
-  const double is = 1.0 / sc;
+  // |x|_1 in [2^ex, 2^(ex+1)), |bc|_1 in [2^eb, 2^(eb+1)); k = max(ex, floor(eb/2)) lies in [-512, 1023].
+  const int k = max(dexp_field(cabs1(x)) - 1023, (dexp_field(cabs1(bc)) - 1023) >> 1);
+  const double is = pow2(-k);
   const double2 xs = cscale(x, is);
-  const double2 bcs = cscale(bc, is * is);
-  double2 y = csqrt_(cadd(cmul(xs, xs), bcs));
+  const double2 bcs = cscale(cscale(bc, is), is);  // bc * 2^-2k in two exact steps
+  const double2 zz = make_double2(fma(xs.x, xs.x, fma(-xs.y, xs.y, bcs.x)), fma(2.0 * xs.x, xs.y, bcs.y));
+  // Principal square root of zz from u = (|zz| + |Re zz|)/2: sqrt(u) and Im zz / (2 sqrt(u)).
+  const double u = 0.5 * (sqrt(fma(zz.x, zz.x, zz.y * zz.y)) + fabs(zz.x));
+  double2 y = make_double2(0.0, 0.0);
+  if (u > 0.0) {
+    const double r = rsqrt(u);
+    const double t = u * r, h = 0.5 * zz.y * r;
+    y = zz.x >= 0.0 ? make_double2(t, h) : make_double2(fabs(h), copysign(t, zz.y));
+  }
   if (fma(xs.x, y.x, xs.y * y.y) < 0.0) y = make_double2(-y.x, -y.y);
   const double2 den = cadd(xs, y);
-  if (den.x == 0.0 && den.y == 0.0) return d;
-  const double2 corr = cdiv(bcs, den);  // scaled by 1/sc
-  return make_double2(d.x - corr.x * sc, d.y - corr.y * sc);
+  const double f = pow2(k) / fma(den.x, den.x, den.y * den.y);
+  // d - (bcs conj(den) / |den|^2) * 2^k
+  const double2 num = make_double2(fma(bcs.x, den.x, bcs.y * den.y), fma(bcs.y, den.x, -bcs.x * den.y));
+  return make_double2(fma(-num.x, f, d.x), fma(-num.y, f, d.y));
 }
 
 }  // namespace tzg
