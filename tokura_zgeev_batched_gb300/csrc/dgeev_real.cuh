@@ -189,14 +189,14 @@ __device__ __forceinline__ void reflect_triples(double* p, int count, int step, 
 // Ahues-Tisseur test for subdiagonal k of the active block (dlahqr's).
 __device__ __forceinline__ bool negligible_real(const RMatView& M, int k, int n, double smlnum) {
   const double h = fabs(*M.at(k, k - 1));
-  if (h <= smlnum) return true;
+  if (nonneg_le(h, smlnum)) return true;
   const double dkk = *M.at(k, k), dk1 = *M.at(k - 1, k - 1);
   double tst = fabs(dk1) + fabs(dkk);
-  if (tst == 0.0) {
+  if (is_zero(tst)) {
     if (k - 2 >= 0) tst += fabs(*M.at(k - 1, k - 2));
     if (k + 1 <= n - 1) tst += fabs(*M.at(k + 1, k));
   }
-  if (h > kUlp * tst) return false;
+  if (nonneg_lt(kUlp * tst, h)) return false;
   const double hu = fabs(*M.at(k - 1, k));
   const double ab = fmax(h, hu), ba = fmin(h, hu);
   const double dd = fabs(dk1 - dkk);
@@ -413,7 +413,7 @@ __device__ int real_qr_eigenvalues(const RMatView& M, const Group<L>& G, Out* __
         const double u3 = h21 * *M.at(c + 2, c + 1);
         const double h00 = fabs(*M.at(c, c - 1)) * (fabs(u2) + fabs(u3));
         const double h01 = fabs(u1) * (fabs(*M.at(c - 1, c - 1)) + fabs(hcc) + fabs(h22));
-        if (h00 <= kUlp * h01) {
+        if (nonneg_le(h00, kUlp * h01)) {
           hit = c;
           break;
         }
@@ -437,10 +437,10 @@ __device__ int real_qr_eigenvalues(const RMatView& M, const Group<L>& G, Out* __
       // reciprocal; tiny or huge norms take the hypot route.
       double t1 = 0.0;
       const double ss = fma(v2, v2, v3 * v3);
-      if (ss != 0.0) {
+      if (!is_zero(ss)) {
         const double nn = fma(v1, v1, ss);
         double xn, rxn;
-        if (nn > 1e-280 && nn < 1e280) {
+        if (nonneg_lt(1e-280, nn) && nonneg_lt(nn, 1e280)) {
           rxn = rsqrt(nn);
           xn = nn * rxn;
         } else {

@@ -294,7 +294,7 @@ __device__ int schur_qr_scaled(const BwdViews& V, const Group<L>& G, const doubl
       const int qend = min(j + 1, i);
       const int tcount = strided_count(G.rank, qend, L);
       const int qcount = strided_count(G.rank, n - 1, L);
-      if (g.c != 0.0) {
+      if (!is_zero(g.c)) {
         double rl, rr2;
         rotation_reciprocals(g.c, u0, u1, v0, v1, rl, rr2);
         const double2 alpha = cscale(g.s, u1 * u1 * rl);
@@ -347,7 +347,8 @@ __device__ int schur_qr_scaled(const BwdViews& V, const Group<L>& G, const doubl
         { const double t = v0; v0 = v1; v1 = t; }
       }
       G.sync();
-      if (u0 < kScaleFloor || u1 < kScaleFloor || v0 < kScaleFloor || v1 < kScaleFloor) {
+      if (nonneg_lt(u0, kScaleFloor) || nonneg_lt(u1, kScaleFloor) || nonneg_lt(v0, kScaleFloor) ||
+          nonneg_lt(v1, kScaleFloor)) {
         // live ranges: row r at columns max(0, r-2) .. n-1; column c of T at rows 0 .. min(c+2, i)
         // (the bulge at c+2) and of Q at every row.
         if (u0 < kScaleFloor) {

@@ -35,6 +35,25 @@ constexpr int kExceptionalPeriod = 10;
 constexpr double kExceptionalWeight = 0.75;
 
 __device__ __forceinline__ double cabs1(double2 z) { return fabs(z.x) + fabs(z.y); }
+
+// Tests on FP64 values done with integer instructions. The FP64 pipe is the
+// bottleneck of every solver here (about 2 FP64 lane-instructions per SM per
+// clock on this GPU), and a floating-point comparison occupies it like an
+// FMA; the integer pipe is idle by comparison. Zero tests ignore the sign bit
+// (-0.0 counts as zero). For non-negative doubles (+0.0 up to +inf) the order
+// of the values is the order of their bit patterns read as signed 64-bit
+// integers; -0.0 reads as negative, below every non-negative value, as a
+// "less than" wants.
+__device__ __forceinline__ bool is_zero(double2 z) {
+  const unsigned long long bits =
+      (unsigned long long)__double_as_longlong(z.x) | (unsigned long long)__double_as_longlong(z.y);
+  return (bits << 1) == 0;
+}
+__device__ __forceinline__ bool is_zero(double x) { return ((unsigned long long)__double_as_longlong(x) << 1) == 0; }
+__device__ __forceinline__ bool nonneg_lt(double a, double b) { return __double_as_longlong(a) < __double_as_longlong(b); }
+__device__ __forceinline__ bool nonneg_le(double a, double b) {
+  return __double_as_longlong(a) <= __double_as_longlong(b);
+}
 __device__ __forceinline__ double2 cadd(double2 a, double2 b) { return make_double2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ double2 csub(double2 a, double2 b) { return make_double2(a.x - b.x, a.y - b.y); }
 __device__ __forceinline__ double2 cmul(double2 a, double2 b) {
@@ -115,11 +134,11 @@ __device__ __forceinline__ Rot make_rot(double2 x, double2 y, double2& rr) {
   const double q = fma(y.x, y.x, y.y * y.y);
   const double nn = p + q;
   const double pn = p * nn;
-  if (q == 0.0) {  // nothing to annihilate (also covers x = y = 0)
+  if (is_zero(q)) {  // nothing to annihilate (also covers x = y = 0)
     g.c = 1.0;
     g.s = make_double2(0.0, 0.0);
     rr = x;
-  } else if (pn < 1e-290) {  // x negligible: swap-like rotation
+  } else if (nonneg_lt(pn, 1e-290)) {  // x negligible: swap-like rotation
     const double rq = rsqrt(q);
     g.c = 0.0;
     g.s = make_double2(y.x * rq, -y.y * rq);  // conj(y)/|y|
@@ -194,7 +213,7 @@ __device__ __forceinline__ int strided_count(int first, int last, int step) {
 // x^2 + bc) and one division in all.
 __device__ __forceinline__ double2 wilkinson_shift(double2 a, double2 b, double2 c, double2 d) {
   const double2 bc = cmul(b, c);
-  if (bc.x == 0.0 && bc.y == 0.0) return d;
+  if (is_zero(bc)) return d;
   const double2 x = make_double2(0.5 * (a.x - d.x), 0.5 * (a.y - d.y));
   // |x|_1 in [2^ex, 2^(ex+1)), |bc|_1 in [2^eb, 2^(eb+1)); k = max(ex, floor(eb/2)) lies in [-512, 1023].
   const int k = max(dexp_field(cabs1(x)) - 1023, (dexp_field(cabs1(bc)) - 1023) >> 1);
@@ -205,12 +224,14 @@ __device__ __forceinline__ double2 wilkinson_shift(double2 a, double2 b, double2
   // Principal square root of zz from u = (|zz| + |Re zz|)/2: sqrt(u) and Im zz / (2 sqrt(u)).
   const double u = 0.5 * (sqrt(fma(zz.x, zz.x, zz.y * zz.y)) + fabs(zz.x));
   double2 y = make_double2(0.0, 0.0);
-  if (u > 0.0) {
+  if (!is_zero(u)) {
     const double r = rsqrt(u);
     const double t = u * r, h = 0.5 * zz.y * r;
-    y = zz.x >= 0.0 ? make_double2(t, h) : make_double2(fabs(h), copysign(t, zz.y));
+    // Re zz = -0.0 takes the second form, which gives the same root then.
+    y = !signbit(zz.x) ? make_double2(t, h) : make_double2(fabs(h), copysign(t, zz.y));
   }
-  if (fma(xs.x, y.x, xs.y * y.y) < 0.0) y = make_double2(-y.x, -y.y);
+  // A zero Re(conj(x) y) of either sign leaves |x + y| the same for both roots.
+  if (signbit(fma(xs.x, y.x, xs.y * y.y))) y = make_double2(-y.x, -y.y);
   const double2 den = cadd(xs, y);
   const double f = pow2(k) / fma(den.x, den.x, den.y * den.y);
   // d - (bcs conj(den) / |den|^2) * 2^k

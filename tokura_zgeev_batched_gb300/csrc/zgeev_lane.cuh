@@ -143,12 +143,6 @@ __device__ __forceinline__ void reflect_vectors(double2* const (&p)[NV], const d
 enum : int { kBalanceNone = 0, kBalancePermute = 1, kBalanceScale = 2, kBalanceBoth = 3 };
 
 // Element helpers shared by the complex (double2) and real (double) views.
-__device__ __forceinline__ bool is_zero(double2 z) {
-  const unsigned long long bits =
-      (unsigned long long)__double_as_longlong(z.x) | (unsigned long long)__double_as_longlong(z.y);
-  return (bits << 1) == 0;  // ignores the sign bits: -0.0 counts as zero
-}
-__device__ __forceinline__ bool is_zero(double x) { return ((unsigned long long)__double_as_longlong(x) << 1) == 0; }
 __device__ __forceinline__ double acc_abs2(double acc, double2 a) { return fma(a.x, a.x, fma(a.y, a.y, acc)); }
 __device__ __forceinline__ double acc_abs2(double acc, double a) { return fma(a, a, acc); }
 __device__ __forceinline__ double2 scaled(double2 a, double f) { return make_double2(a.x * f, a.y * f); }
@@ -375,15 +369,15 @@ __device__ __forceinline__ bool negligible_subdiag(const MatView& M, int k, int 
                                                    double tol = kUlp) {
   const double2 hk = *M.at(k, k - 1);
   const double h1 = cabs1(hk);
-  if (h1 <= smlnum) return true;
+  if (nonneg_le(h1, smlnum)) return true;
   const double2 dkk = *M.at(k, k);
   const double2 dk1 = *M.at(k - 1, k - 1);
   double tst = cabs1(dk1) + cabs1(dkk);
-  if (tst == 0.0) {
+  if (is_zero(tst)) {
     if (k - 2 >= lo) tst += cabs1(*M.at(k - 1, k - 2));
     if (k + 1 <= hi) tst += cabs1(*M.at(k + 1, k));
   }
-  if (h1 > tol * tst) return false;
+  if (nonneg_lt(tol * tst, h1)) return false;
   const double2 up = *M.at(k - 1, k);
   const double hu = cabs1(up);
   const double ab = fmax(h1, hu), ba = fmin(h1, hu);

@@ -55,7 +55,7 @@ __device__ __forceinline__ void rotation_reciprocals(double c, double u0, double
                                                      double& rr) {
   const double pl = c * u0 * u1, pr = c * v0 * v1;
   const double prod = pl * pr;
-  if (prod > 1e-290) {
+  if (nonneg_lt(1e-290, prod)) {
     const double inv = 1.0 / prod;
     rl = inv * pr;
     rr = inv * pl;
@@ -103,15 +103,15 @@ __device__ __forceinline__ bool negligible_subdiag_scaled(const MatView& M, int 
                                                           double tol = kUlp) {
   const double2 sk = *scale_slot(M, k), sk1 = *scale_slot(M, k - 1);
   const double h1 = cabs1(*M.at(k, k - 1)) * (sk.x * sk1.y);
-  if (h1 <= smlnum) return true;
+  if (nonneg_le(h1, smlnum)) return true;
   const double2 dkk = cscale(*M.at(k, k), sk.x * sk.y);
   const double2 dk1 = cscale(*M.at(k - 1, k - 1), sk1.x * sk1.y);
   double tst = cabs1(dk1) + cabs1(dkk);
-  if (tst == 0.0) {
+  if (is_zero(tst)) {
     if (k - 2 >= lo) tst += cabs1(*M.at(k - 1, k - 2)) * (sk1.x * scale_slot(M, k - 2)->y);
     if (k + 1 <= hi) tst += cabs1(*M.at(k + 1, k)) * (scale_slot(M, k + 1)->x * sk.y);
   }
-  if (h1 > tol * tst) return false;
+  if (nonneg_lt(tol * tst, h1)) return false;
   const double hu = cabs1(*M.at(k - 1, k)) * (sk1.x * sk.y);
   const double ab = fmax(h1, hu), ba = fmin(h1, hu);
   const double dd = cabs1(csub(dk1, dkk));
@@ -217,7 +217,7 @@ __device__ int qr_eigenvalues_scaled(const MatView& M, const Group<L>& G, Out* _
       const int c0 = j + G.rank;
       const int qend = min(j + 1, i);
       const int q0 = lo + G.rank;
-      if (g.c != 0.0) {
+      if (!is_zero(g.c)) {
         // Left: rows (j, j+1) over columns j .. i (and j-1, whose row j+1 entry is annihilated).
         double rl, rr2;
         rotation_reciprocals(g.c, u0, u1, v0, v1, rl, rr2);
@@ -271,7 +271,8 @@ __device__ int qr_eigenvalues_scaled(const MatView& M, const Group<L>& G, Out* _
       G.sync();
       // Rescale factors that fell below 2^-60 (group-uniform decision) over the live
       // entries: row r at columns max(lo, r-2) .. i, column c at rows lo .. min(c+2, i).
-      if (u0 < kScaleFloor || u1 < kScaleFloor || v0 < kScaleFloor || v1 < kScaleFloor) {
+      if (nonneg_lt(u0, kScaleFloor) || nonneg_lt(u1, kScaleFloor) || nonneg_lt(v0, kScaleFloor) ||
+          nonneg_lt(v1, kScaleFloor)) {
         if (u0 < kScaleFloor) {
           for (int c = max(lo, j - 2) + G.rank; c <= i; c += L) *M.at(j, c) = cscale(*M.at(j, c), u0);
           u0 = 1.0;
