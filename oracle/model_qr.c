@@ -492,7 +492,7 @@ void model_estimates_batched(int n, int batch, const double* A, float* est, floa
  * c: two complex multiply-adds per element pair (8 FP64 operations) instead of
  * the 12 of the plain rotation. Shifts, rotations and deflation tests read the
  * true entries through the scale factors; a row or column whose factor leaves
- * [2^-60, 2^60] is rescaled to 1 (O(n) work, counted). */
+ * [2^-150, 2^150] is rescaled to 1 (O(n) work, counted). */
 #define HT(r, c) zscale(H(r, c), dc[c] / dr[r])
 
 static int negligible_s(int n, const zc* a, const double* dr, const double* dc, int k, int lo, int hi,
@@ -535,7 +535,7 @@ static int qr_scaled(int n, zc* a, zc* w, const float* est, unsigned char* used,
   double dr[64], dc[64]; /* the library's orders: n <= 64 */
   if (n > 64) return 1;
   for (int k = 0; k < n; ++k) { used[k] = 0; dr[k] = dc[k] = 1.0; }
-  const double big = 0x1p60, small = 0x1p-60;
+  const double big = 0x1p150, small = 0x1p-150;
   for (;;) {
     for (;;) {
       int hit = lo;

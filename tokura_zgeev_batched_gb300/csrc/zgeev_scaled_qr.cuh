@@ -16,8 +16,17 @@
 // (rot_left / rot_right). The rounding error of an update, scaled back to H,
 // is eps * (c |H(j, :)| + |s| |H(j+1, :)|): the same bound as the plain
 // rotation's. Factors only shrink (c <= 1); a row or column whose factor
-// falls below 2^-60 is multiplied into K over its live entries and reset to 1
-// (a few hundred O(n) rescales per 64 x 64 matrix). An exact swap (c = 0)
+// falls below 2^-150 is multiplied into K over its live entries and reset to 1
+// (an O(n) rescale, 46 per 64 x 64 Gaussian matrix with hints). The floor is
+// low because a rescale runs in the lanes that need it while the rest of the
+// warp waits: at 2^-60 (185 rescales per matrix) a rescale somewhere in the
+// warp came with most rotations and cost the QR phase about a tenth of its
+// FP64 lane slots. It is high enough for every product to stay finite: the
+// pre-scaled matrix has entries below 2^61 and Frobenius norm below 2^68,
+// make_rot's c is at least 2^-482 / ||H||_F^2 > 2^-618 (below, the rotation
+// is a swap), so K stays below 2^368 and the largest intermediate (the
+// updated K(j, :) of a rotation with the smallest c, before its rescale)
+// below 2^990. An exact swap (c = 0)
 // exchanges the two factors and applies s directly. Entries outside the
 // active block keep stale factors; the only one read again, the negligible
 // subdiagonal entry where the block splits from the rows above, is stored as
@@ -42,14 +51,14 @@ namespace tzg {
 // 3..n-1 of column 0 and 4..6 of column 1).
 constexpr int kScaledMinN = 7;
 // Rescale threshold of a row or column factor.
-constexpr double kScaleFloor = 8.673617379884035472e-19;  // 2^-60
+constexpr double kScaleFloor = 0x1p-150;
 
 __device__ __forceinline__ double2* scale_slot(const MatView& M, int k) {
   return k <= M.n - 4 ? M.at(k + 3, 0) : M.at(k - M.n + 7, 1);
 }
 
 // 1/(c u0 u1) and 1/(c v0 v1) from one reciprocal of their product when it
-// stays normal (c and the factors can each be as small as ~1e-145 and 2^-60),
+// stays normal (c and the factors can each be as small as ~2^-618 and 2^-150),
 // else from two.
 __device__ __forceinline__ void rotation_reciprocals(double c, double u0, double u1, double v0, double v1, double& rl,
                                                      double& rr) {
@@ -269,7 +278,7 @@ __device__ int qr_eigenvalues_scaled(const MatView& M, const Group<L>& G, Out* _
         { const double t = v0; v0 = v1; v1 = t; }
       }
       G.sync();
-      // Rescale factors that fell below 2^-60 (group-uniform decision) over the live
+      // Rescale factors that fell below 2^-150 (group-uniform decision) over the live
       // entries: row r at columns max(lo, r-2) .. i, column c at rows lo .. min(c+2, i).
       if (nonneg_lt(u0, kScaleFloor) || nonneg_lt(u1, kScaleFloor) || nonneg_lt(v0, kScaleFloor) ||
           nonneg_lt(v1, kScaleFloor)) {
