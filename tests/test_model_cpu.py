@@ -159,6 +159,19 @@ def test_model_scaled_rotations(gen, n):
         assert resc.sum() <= 8 * s.sum()  # a few row/column rescales per sweep at most
 
 
+def test_model_scaled_rescales_are_rare():
+    """With the factor floor at 2^-150 a 64x64 Gaussian matrix needs a few dozen O(n)
+    rescales over its ~170 sweeps (185 at a 2^-60 floor). On the GPU a rescale runs only in the
+    lanes whose factor fell below the floor while the rest of the warp waits, so their number,
+    not their own arithmetic, is what they cost."""
+    A = wl.gaussian(64, 64, seed=5)
+    est = lo.model_estimates(A)
+    _, f, s, _, resc = lo.model_qr_variant(A, est, scaled=True)
+    assert (f == 0).all()
+    assert 20 <= resc.mean() <= 80, resc.mean()
+    assert resc.mean() <= 0.5 * s.mean()  # fewer than one rescale every other sweep
+
+
 @pytest.mark.parametrize("gen", ["gaussian", "vdv", "companion", "uniform"])
 def test_model_elementary_hessenberg(gen):
     """Hessenberg form by stabilized elementary similarity transforms (half the multiply-adds):
