@@ -86,6 +86,15 @@ TOKURA_API int tokuraSetPlainConfig(tokurablas_t* handle, int n, int lanes_per_m
 TOKURA_API int tokuraGetPlainConfig(const tokurablas_t* handle, int n, int batch_count, int* lanes_per_matrix,
                                     int* threads_per_block);
 
+/* Lanes per matrix of the QR phase of plain calls of order n that use shift
+ * hints (tokuraSetShiftHints), where staging + Hessenberg and the QR are two
+ * launches: 1, 2, 4 or 8, or 0 for the library's choice (the width of the
+ * first launch, except two lanes after a four-lane first launch for n <= 24).
+ * Fewer lanes than the first launch means fewer instructions per matrix
+ * spent on rotation generation and shifts, in fewer, fuller warps.
+ * Returns 0, -1 NULL handle, -2 n out of range, -3 bad lanes. */
+TOKURA_API int tokuraSetPlainQrLanes(tokurablas_t* handle, int n, int lanes_per_matrix);
+
 /* Autotuner (replaces the reference's build-time tuner,
  * src/TOKURA_ZHSEQR_BATCHED_GEHRD_TUNING_main.cu:89-227, and its generated
  * tables). For each order n in [n_min, n_max], times every plain-kernel shape

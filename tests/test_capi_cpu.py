@@ -290,6 +290,7 @@ def test_null_handle_is_rejected_first(lib):
     assert lib.tokuraAutotune(None, 1, 2, 10, None) == -1
     assert lib.tokuraAutotuneRagged(None, 10, 1, 64, None) == -1
     assert lib.tokuraSetPlainConfig(None, 8, 1, 32) == -1
+    assert lib.tokuraSetPlainQrLanes(None, 8, 2) == -1
     assert lib.tokuraGetPlainConfig(None, 8, 10, ctypes.byref(lanes), ctypes.byref(threads)) == -1
     assert lib.tokuraSaveTuning(None, b"/nonexistent/t") == -1 and lib.tokuraLoadTuning(None, b"/nonexistent/t") == -1
     assert lib.tokura_zgeev_backward_gpu(None, 8, 1, p, p, p, p, p, p, None) == -1

@@ -33,6 +33,7 @@ _SIGNATURES = {
     ),
     "tokuraSetSweepCap": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int]),
     "tokuraSetPlainConfig": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+    "tokuraSetPlainQrLanes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]),
     "tokuraGetPlainConfig": (
         ctypes.c_int,
         [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)],
@@ -151,6 +152,10 @@ class Handle:
 
     def set_plain_config(self, n: int, lanes: int, threads: int) -> int:
         return int(lib().tokuraSetPlainConfig(self.ptr, int(n), int(lanes), int(threads)))
+
+    def set_plain_qr_lanes(self, n: int, lanes: int) -> int:
+        """Lanes per matrix of the hinted QR phase for order n (0: as the first launch)."""
+        return int(lib().tokuraSetPlainQrLanes(self.ptr, int(n), int(lanes)))
 
     def plain_config(self, n: int, batch: int) -> tuple[int, int]:
         lanes, threads = ctypes.c_int(), ctypes.c_int()

@@ -103,6 +103,16 @@ extern "C" int tokuraSetPlainConfig(tokurablas_t* handle, int n, int lanes_per_m
   return 0;
 }
 
+extern "C" int tokuraSetPlainQrLanes(tokurablas_t* handle, int n, int lanes_per_matrix) {
+  if (handle == nullptr) return -1;
+  if (!(n > 0 && n <= TOKURA_ZGEEV_BATCHED_MAX_MATRIX_SIZE)) return -2;
+  if (!(lanes_per_matrix == 0 || lanes_per_matrix == 1 || lanes_per_matrix == 2 || lanes_per_matrix == 4 ||
+        lanes_per_matrix == 8))
+    return -3;
+  handle->plain_qr_lanes[n] = lanes_per_matrix;
+  return 0;
+}
+
 extern "C" int tokuraSetRealConfig(tokurablas_t* handle, int n, int lanes_per_matrix, int threads_per_block) {
   if (handle == nullptr) return -1;
   if (!(n > 0 && n <= TOKURA_ZGEEV_BATCHED_MAX_MATRIX_SIZE)) return -2;

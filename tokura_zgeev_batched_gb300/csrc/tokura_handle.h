@@ -37,6 +37,7 @@ struct tokurablas_t {
   int itmax_override = 0;  // >0 replaces the per-eigenvalue sweep cap 30*max(10,n)
   // Tuned plain-kernel shape per n (index 1..64); lanes == 0 means "heuristic".
   tzg::PlainConfig plain[65] = {};
+  int plain_qr_lanes[65] = {};     // lanes per matrix of the hinted QR phase per n; 0 = chosen per call
   tzg::PlainConfig real[65] = {};  // the same for the real (dgeev/sgeev) kernel
   int ragged_lanes = 0;  // lanes per matrix of the ragged solvers; 0 = chosen per launch
   int balance_mode = 0;  // balancing before the eigenvalue solves: 0 none (the reference's behaviour) .. 3 both
@@ -91,6 +92,12 @@ inline PlainConfig plain_config_for(const tokurablas_t* h, int n, int batch) {
   }
   if (c.threads == 0) c.threads = 32;
   c.scaled = n >= scaled_threshold(h, c.lanes) ? 1 : 0;
+  // The hinted QR phase of four-lane launches runs at two lanes from n = 12 (the
+  // hints' threshold) to 24: 10,000 matrices at n = 12 / 16 / 24 took 2.08 / 3.99
+  // / 10.42 ms, 1.89 / 3.70 / 9.66 ms so; at n = 32 20.69 against 20.78 ms, at
+  // n = 48 and 64 two lanes were 11-23 % slower.
+  c.qr_lanes = h->plain_qr_lanes[n] > 0 ? h->plain_qr_lanes[n] : (c.lanes == 4 && n <= 24 ? 2 : c.lanes);
+  c.scaled_qr = n >= scaled_threshold(h, c.qr_lanes) ? 1 : 0;
   return c;
 }
 

@@ -109,6 +109,8 @@ extern "C" TOKURA_API int tokuraAutotune(tokurablas_t* handle, int n_min, int n_
       for (int ti = 0; ti < 4; ++ti) {
         PlainConfig cfg{kLanes[li], kThreads[ti]};
         cfg.scaled = n >= scaled_threshold(handle, cfg.lanes) ? 1 : 0;
+        cfg.qr_lanes = cfg.lanes;
+        cfg.scaled_qr = cfg.scaled;
         cudaError_t err;
         const float ms = time_launches(stream, 2, [&]() {
           return launch_plain(cfg, n, batch_count, A, eig, work, flag, default_itmax(n), stream, 0,

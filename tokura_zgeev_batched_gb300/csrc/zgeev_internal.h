@@ -14,6 +14,8 @@ struct PlainConfig {
   int lanes;            // lanes per matrix: 1, 2, 4 or 8
   int threads;          // threads per block (multiple of 32)
   int scaled = 0;       // QR with scaled rotations (orders >= 7; zgeev_scaled_qr.cuh)
+  int qr_lanes = 0;     // lanes per matrix of the QR phase when it is its own launch (shift hints); 0: `lanes`
+  int scaled_qr = 0;    // `scaled` for the QR phase at qr_lanes
 };
 
 // Iteration cap per eigenvalue: LAPACK's rule 30*max(10, n) unless overridden.

@@ -82,23 +82,24 @@ struct Complex64Batch {
 
 // `scaled` (nonzero, n >= kScaledMinN) selects the QR with scaled rotations
 // (zgeev_scaled_qr.cuh) for the QR part; the prepare part does not depend on it.
+// Warp w solves matrices w*32/L .. w*32/L + 32/L - 1 with L lanes each. The
+// staging area holds the batch in tiles of `stage_tw` matrices (32/L of the
+// launch that staged it): the QR phase may run at fewer lanes per matrix than
+// the prepare phase, a warp then spanning several staging tiles.
 template <int L, bool kBalance, int kPhase, class Batch>
 __global__ void __launch_bounds__(256) zgeev_plain_kernel(int n, int batch, Batch B, double2* __restrict__ work,
                                                            char* __restrict__ flag, int itmax, int balance,
                                                            const float2* __restrict__ est, int* __restrict__ state,
-                                                           int scaled) {
+                                                           int scaled, int stage_tw) {
   constexpr int TW = 32 / L;
   const int lane = threadIdx.x & 31;
   const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const long long g0 = warp * TW;
-  if (g0 >= batch) return;  // warp-uniform
-  const int tw = (int)min((long long)TW, (long long)batch - g0);
-  const int slot = lane / L;
-  if (slot >= tw) return;  // whole lane groups leave together; no warp-wide barriers follow
+  const long long j = warp * TW + lane / L;
+  if (j >= batch) return;  // whole lane groups leave together; no warp-wide barriers follow
   const Group<L> G;
   const long long nn = (long long)n * n;
-  const long long j = g0 + slot;
-  MatView M{work + g0 * nn + slot, n, tw};
+  const long long t0 = j / stage_tw * stage_tw;  // first matrix of j's staging tile
+  MatView M{work + t0 * nn + (j - t0), n, (int)min((long long)stage_tw, (long long)batch - t0)};
 
   if (kPhase != kPhaseQR && !B.valid(j)) {  // NULL matrix pointer: NaN eigenvalues, flag 3 (group-uniform)
     const double nan = __longlong_as_double(0x7ff8000000000000LL);
@@ -148,14 +149,14 @@ __global__ void __launch_bounds__(256) zgeev_plain_kernel(int n, int batch, Batc
 template <int L, bool kBalance, int kPhase, class Batch>
 inline cudaError_t launch_plain_l(unsigned blocks, int threads, cudaStream_t stream, int n, int batch,
                                   const Batch& B, double2* work, char* flag, int itmax, int balance,
-                                  const float2* est, int* state, int carveout, int scaled) {
+                                  const float2* est, int* state, int carveout, int scaled, int stage_tw) {
   if (kPhase != kPhaseAll) {  // shared memory for estimators running beside (this or another call's)
     const cudaError_t err = cudaFuncSetAttribute(zgeev_plain_kernel<L, kBalance, kPhase, Batch>,
                                                  cudaFuncAttributePreferredSharedMemoryCarveout, carveout);
     if (err != cudaSuccess) return err;
   }
   zgeev_plain_kernel<L, kBalance, kPhase, Batch>
-      <<<blocks, threads, 0, stream>>>(n, batch, B, work, flag, itmax, balance, est, state, scaled);
+      <<<blocks, threads, 0, stream>>>(n, batch, B, work, flag, itmax, balance, est, state, scaled, stage_tw);
   return cudaGetLastError();
 }
 
@@ -164,31 +165,31 @@ inline cudaError_t launch_plain_l(unsigned blocks, int threads, cudaStream_t str
 template <int kPhase, class Batch>
 inline cudaError_t launch_plain_phase(int L, bool bal, unsigned blocks, int threads, cudaStream_t stream, int n,
                                       int batch, const Batch& B, double2* work, char* flag, int itmax, int balance,
-                                      const float2* est, int* state, int carveout, int scaled) {
+                                      const float2* est, int* state, int carveout, int scaled, int stage_tw) {
   constexpr bool kB = kPhase != kPhaseQR;  // balanced instantiation exists
   const bool b = bal && kB;
   const int bv = b ? balance : 0;
   switch (L) {
     case 1:
       return b ? launch_plain_l<1, kB, kPhase>(blocks, threads, stream, n, batch, B, work, flag, itmax, bv, est, state,
-                                                        carveout, scaled)
+                                                        carveout, scaled, stage_tw)
                : launch_plain_l<1, false, kPhase>(blocks, threads, stream, n, batch, B, work, flag, itmax, 0, est, state,
-                                                           carveout, scaled);
+                                                           carveout, scaled, stage_tw);
     case 2:
       return b ? launch_plain_l<2, kB, kPhase>(blocks, threads, stream, n, batch, B, work, flag, itmax, bv, est, state,
-                                                        carveout, scaled)
+                                                        carveout, scaled, stage_tw)
                : launch_plain_l<2, false, kPhase>(blocks, threads, stream, n, batch, B, work, flag, itmax, 0, est, state,
-                                                           carveout, scaled);
+                                                           carveout, scaled, stage_tw);
     case 4:
       return b ? launch_plain_l<4, kB, kPhase>(blocks, threads, stream, n, batch, B, work, flag, itmax, bv, est, state,
-                                                        carveout, scaled)
+                                                        carveout, scaled, stage_tw)
                : launch_plain_l<4, false, kPhase>(blocks, threads, stream, n, batch, B, work, flag, itmax, 0, est, state,
-                                                           carveout, scaled);
+                                                           carveout, scaled, stage_tw);
     case 8:
       return b ? launch_plain_l<8, kB, kPhase>(blocks, threads, stream, n, batch, B, work, flag, itmax, bv, est, state,
-                                                        carveout, scaled)
+                                                        carveout, scaled, stage_tw)
                : launch_plain_l<8, false, kPhase>(blocks, threads, stream, n, batch, B, work, flag, itmax, 0, est, state,
-                                                           carveout, scaled);
+                                                           carveout, scaled, stage_tw);
     default:
       return cudaErrorInvalidValue;
   }
@@ -201,26 +202,32 @@ template <class Batch>
 cudaError_t launch_batch(const PlainConfig& cfg, int n, int batch, const Batch& B, double2* work, char* flag,
                          int itmax, cudaStream_t stream, int balance, bool hints, const ForkJoin* fj) {
   const int L = cfg.lanes;
-  if (!(L == 1 || L == 2 || L == 4 || L == 8)) return cudaErrorInvalidValue;
+  // Lanes per matrix of the QR phase when it runs as its own launch (with hints).
+  const int Lq = cfg.qr_lanes > 0 ? cfg.qr_lanes : L;
+  auto valid_lanes = [](int l) { return l == 1 || l == 2 || l == 4 || l == 8; };
+  if (!valid_lanes(L) || !valid_lanes(Lq)) return cudaErrorInvalidValue;
   const int tw = 32 / L;
-  const long long warps = ((long long)batch + tw - 1) / tw;
   const int threads = cfg.threads;
   if (threads < 32 || threads > 256 || threads % 32 != 0) return cudaErrorInvalidValue;
-  const long long blocks = (warps * 32 + threads - 1) / threads;
-  if (blocks > 0x7fffffffLL) return cudaErrorInvalidValue;
+  auto blocks_for = [&](int lanes) {
+    const long long warps = ((long long)batch + 32 / lanes - 1) / (32 / lanes);
+    return (warps * 32 + threads - 1) / threads;
+  };
+  const long long blocks = blocks_for(L), blocks_q = blocks_for(Lq);
+  if (blocks > 0x7fffffffLL || blocks_q > 0x7fffffffLL) return cudaErrorInvalidValue;
   const bool bal = balance != 0;
   const int scaled = cfg.scaled;
   constexpr int kDef = cudaSharedmemCarveoutDefault;
   if (!hints)
     return launch_plain_phase<kPhaseAll>(L, bal, (unsigned)blocks, threads, stream, n, batch, B, work, flag, itmax,
-                                         balance, nullptr, nullptr, kDef, scaled);
+                                         balance, nullptr, nullptr, kDef, scaled, tw);
   float2* est = reinterpret_cast<float2*>(work + (size_t)n * n * batch);
   int* state = reinterpret_cast<int*>(est + (size_t)n * batch);
   cudaError_t err;
   if (fj == nullptr || fj->aux == nullptr) {  // no second stream: estimator first, then one kernel
     if ((err = launch_estimates(n, batch, B, est, stream)) != cudaSuccess) return err;
     return launch_plain_phase<kPhaseAll>(L, bal, (unsigned)blocks, threads, stream, n, batch, B, work, flag, itmax,
-                                         balance, est, nullptr, kDef, scaled);
+                                         balance, est, nullptr, kDef, scaled, tw);
   }
   std::lock_guard<std::mutex> lock(*fj->mu);
   if ((err = cudaEventRecord(fj->fork, stream)) != cudaSuccess) return err;
@@ -229,12 +236,12 @@ cudaError_t launch_batch(const PlainConfig& cfg, int n, int batch, const Batch& 
   if ((err = cudaEventRecord(fj->join, fj->aux)) != cudaSuccess) return err;
   if ((err = launch_plain_phase<kPhasePrepare>(L, bal, (unsigned)blocks, threads, stream, n, batch, B, work, flag,
                                                itmax, balance, nullptr, state, cudaSharedmemCarveoutMaxShared,
-                                               scaled)) !=
+                                               scaled, tw)) !=
       cudaSuccess)
     return err;
   if ((err = cudaStreamWaitEvent(stream, fj->join, 0)) != cudaSuccess) return err;
-  return launch_plain_phase<kPhaseQR>(L, false, (unsigned)blocks, threads, stream, n, batch, B, work, flag, itmax, 0,
-                                      est, state, cudaSharedmemCarveoutMaxShared, scaled);
+  return launch_plain_phase<kPhaseQR>(Lq, false, (unsigned)blocks_q, threads, stream, n, batch, B, work, flag, itmax,
+                                      0, est, state, cudaSharedmemCarveoutMaxShared, cfg.scaled_qr, tw);
 }
 
 }  // namespace tzg
