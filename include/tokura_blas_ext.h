@@ -75,8 +75,8 @@ TOKURA_API int tokuraSetScaledRotations(tokurablas_t* handle, int min_order);
  * Returns 0, -1 NULL handle, -2 n outside 1..65. */
 TOKURA_API int tokuraSetRaggedHintMinOrder(tokurablas_t* handle, int n);
 
-/* Launch shape of the plain kernel for order n: lanes per matrix (1, 2, 4, 8;
- * 0 = choose from the batch size) and threads per block (32..256, multiple
+/* Launch shape of the plain kernel for order n: lanes per matrix (1, 2, 4, 8,
+ * 16, 32; 0 = choose from the batch size) and threads per block (32..256, multiple
  * of 32; 0 = 32). Replaces the reference's compile-time tables
  * (include/tokura_zhseqr_parameters.h, tokura_zgeev_batched.cu:13-60).
  * Returns 0, -1 NULL handle, -2 n out of range, -3 bad lanes, -4 bad threads. */
@@ -88,7 +88,7 @@ TOKURA_API int tokuraGetPlainConfig(const tokurablas_t* handle, int n, int batch
 
 /* Lanes per matrix of the QR phase of plain calls of order n that use shift
  * hints (tokuraSetShiftHints), where staging + Hessenberg and the QR are two
- * launches: 1, 2, 4 or 8, or 0 for the library's choice (the width of the
+ * launches: 1, 2, 4, 8, 16 or 32, or 0 for the library's choice (the width of the
  * first launch, except two lanes after a four-lane first launch for n <= 24).
  * Fewer lanes than the first launch means fewer instructions per matrix
  * spent on rotation generation and shifts, in fewer, fuller warps.
@@ -98,7 +98,7 @@ TOKURA_API int tokuraSetPlainQrLanes(tokurablas_t* handle, int n, int lanes_per_
 /* Autotuner (replaces the reference's build-time tuner,
  * src/TOKURA_ZHSEQR_BATCHED_GEHRD_TUNING_main.cu:89-227, and its generated
  * tables). For each order n in [n_min, n_max], times every plain-kernel shape
- * (lanes per matrix 1/2/4/8 x threads per block 32/64/128/256) on batch_count
+ * (lanes per matrix 1/2/4/8/16/32 x threads per block 32/64/128/256) on batch_count
  * seeded synthetic complex Gaussian matrices and stores the fastest in the
  * handle. Allocates its own scratch (cudaMalloc), synchronizes `stream`.
  * Returns 0; -1 NULL handle, -2 bad range, -6 batch_count <= 0,

@@ -50,7 +50,7 @@ def main():
         return A, w, f
 
     for n in (1, 2, 3, 17, 33, 64):
-        for lanes in (1, 4):
+        for lanes in (1, 4, 32):
             check(f"plain_n{n}_L{lanes}", lambda: plain(n, 96, 10 + n, lanes=lanes))
     check("plain_balance_n40", lambda: plain(40, 64, 7, balance=3))
     # sweeps against the CPU model of the iteration: no hints, plain and scaled rotations

@@ -59,5 +59,6 @@ def test_setter_validates(cuda):
     assert h.set_plain_qr_lanes(0, 2) == -2
     assert h.set_plain_qr_lanes(65, 2) == -2
     assert h.set_plain_qr_lanes(16, 3) == -3
-    assert h.set_plain_qr_lanes(16, 16) == -3
+    assert h.set_plain_qr_lanes(16, 64) == -3
+    assert h.set_plain_qr_lanes(16, 32) == 0
     assert h.set_plain_qr_lanes(16, 0) == 0

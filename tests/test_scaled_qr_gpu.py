@@ -39,7 +39,7 @@ def test_setter_validation(cuda):
     assert h.set_scaled_rotations(0) == -2 and h.set_scaled_rotations(66) == -2
 
 
-@pytest.mark.parametrize("lanes", [1, 2, 4, 8])
+@pytest.mark.parametrize("lanes", [1, 2, 4, 8, 16, 32])
 @pytest.mark.parametrize("n", [7, 8, 13, 24, 32, 47, 64])
 def test_gaussian_every_lane_width(cuda, n, lanes):
     A = wl.gaussian(256, n, seed=3100 + n + lanes)

@@ -94,9 +94,7 @@ extern "C" int tokuraSetSweepCap(tokurablas_t* handle, int cap) {
 extern "C" int tokuraSetPlainConfig(tokurablas_t* handle, int n, int lanes_per_matrix, int threads_per_block) {
   if (handle == nullptr) return -1;
   if (!(n > 0 && n <= TOKURA_ZGEEV_BATCHED_MAX_MATRIX_SIZE)) return -2;
-  if (!(lanes_per_matrix == 0 || lanes_per_matrix == 1 || lanes_per_matrix == 2 || lanes_per_matrix == 4 ||
-        lanes_per_matrix == 8))
-    return -3;
+  if (!tzg::plain_lanes_valid(lanes_per_matrix, true)) return -3;
   if (!(threads_per_block == 0 || (threads_per_block >= 32 && threads_per_block <= 256 && threads_per_block % 32 == 0)))
     return -4;
   handle->plain[n] = PlainConfig{lanes_per_matrix, threads_per_block};
@@ -106,9 +104,7 @@ extern "C" int tokuraSetPlainConfig(tokurablas_t* handle, int n, int lanes_per_m
 extern "C" int tokuraSetPlainQrLanes(tokurablas_t* handle, int n, int lanes_per_matrix) {
   if (handle == nullptr) return -1;
   if (!(n > 0 && n <= TOKURA_ZGEEV_BATCHED_MAX_MATRIX_SIZE)) return -2;
-  if (!(lanes_per_matrix == 0 || lanes_per_matrix == 1 || lanes_per_matrix == 2 || lanes_per_matrix == 4 ||
-        lanes_per_matrix == 8))
-    return -3;
+  if (!tzg::plain_lanes_valid(lanes_per_matrix, true)) return -3;
   handle->plain_qr_lanes[n] = lanes_per_matrix;
   return 0;
 }
@@ -204,7 +200,7 @@ extern "C" int tokura_zgeev_backward_gpu(tokurablas_t* handle, int n, int batch_
   if (!(batch_count > 0)) return -6;
   if (flag == nullptr) return -7;
   if (grad_A == nullptr) return -8;
-  const int lanes = tzg::plain_config_for(handle, n, batch_count).lanes;
+  const int lanes = tzg::group_lanes_for(handle, n, batch_count);
   const int itmax = handle->itmax_override > 0 ? handle->itmax_override : tzg::default_itmax(n);
   const cudaError_t err = tzg::launch_backward(
       lanes, n, batch_count, reinterpret_cast<const double2*>(A), reinterpret_cast<const double2*>(eigenvalues),
@@ -260,7 +256,7 @@ extern "C" int tokura_zgeev_vectors_batched_gpu(tokurablas_t* handle, int n, int
   if (work == nullptr) return -5;
   if (!(batch_count > 0)) return -6;
   if (flag == nullptr) return -7;
-  const int lanes = tzg::plain_config_for(handle, n, batch_count).lanes;
+  const int lanes = tzg::group_lanes_for(handle, n, batch_count);
   const int itmax = handle->itmax_override > 0 ? handle->itmax_override : tzg::default_itmax(n);
   const cudaError_t err = tzg::launch_vectors(
       lanes, n, batch_count, reinterpret_cast<const double2*>(A), reinterpret_cast<double2*>(eigenvalues),

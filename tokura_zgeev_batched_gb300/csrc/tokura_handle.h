@@ -78,16 +78,34 @@ inline int scaled_threshold(const tokurablas_t* h, int lanes) {
   return t < 7 ? 7 : (t > 65 ? 65 : t);
 }
 
+// Lane widths of the complex plain kernel (0 = chosen per call where allowed).
+inline bool plain_lanes_valid(int lanes, bool allow_zero) {
+  return (allow_zero && lanes == 0) || lanes == 1 || lanes == 2 || lanes == 4 || lanes == 8 || lanes == 16 ||
+         lanes == 32;
+}
+
 inline PlainConfig plain_config_for(const tokurablas_t* h, int n, int batch) {
   PlainConfig c = h->plain[n];
   if (c.lanes == 0) {
+    // Batches below a quarter of the lanes that fill the GPU spread each matrix
+    // over more lanes, up to n/2 (two elements of a row or column per lane) and 32:
+    // 304 matrices at n = 64 (two per SM) took 73.4 ms at 4 lanes and 21.7 ms at
+    // 32, 2,432 at n = 64 53.9 ms at 8 and 50.5 at 16, 1,216 at n = 32 8.1 ms at
+    // 8 and 6.4 at 16 (8.4 at 32); at 65,536 matrices 32 lanes were 3.1x slower
+    // than one, every lane of a warp then computing each rotation and shift.
     const long long want_lanes = (long long)h->sm_count * 4 * 2 * 32;
     if ((long long)batch >= want_lanes)
       c.lanes = 1;
     else if ((long long)batch * 2 >= want_lanes)
       c.lanes = 2;
-    else
+    else if ((long long)batch * 4 >= want_lanes)
       c.lanes = 4;
+    else {
+      int cap = 32;
+      while (cap > 4 && cap > n / 2) cap >>= 1;
+      c.lanes = 4;
+      while (c.lanes < cap && (long long)batch * c.lanes < want_lanes) c.lanes <<= 1;
+    }
     if (n <= 2) c.lanes = 1;
   }
   if (c.threads == 0) c.threads = 32;
@@ -99,6 +117,13 @@ inline PlainConfig plain_config_for(const tokurablas_t* h, int n, int batch) {
   c.qr_lanes = h->plain_qr_lanes[n] > 0 ? h->plain_qr_lanes[n] : (c.lanes == 4 && n <= 24 ? 2 : c.lanes);
   c.scaled_qr = n >= scaled_threshold(h, c.qr_lanes) ? 1 : 0;
   return c;
+}
+
+// Lanes per matrix of the gradient and eigenvector kernels (instantiated for
+// 1, 2, 4 and 8 lanes): the plain call's choice, at most 8.
+inline int group_lanes_for(const tokurablas_t* h, int n, int batch) {
+  const int l = plain_config_for(h, n, batch).lanes;
+  return l > 8 ? 8 : l;
 }
 
 // Launch shape of the real kernel: a tuned entry, else the lane heuristic of

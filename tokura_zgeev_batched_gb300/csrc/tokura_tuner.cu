@@ -4,7 +4,7 @@
 // TUNING_main.cu:89-227, which timed threads-per-matrix for each n once on
 // 8192 random matrices and wrote #define tables that were compiled into the
 // library, include/tokura_zhseqr_parameters.h). Here the candidates — lanes
-// per matrix (1, 2, 4, 8) x threads per block (32, 64, 128, 256) — are timed with
+// per matrix (1 to 32) x threads per block (32, 64, 128, 256) — are timed with
 // CUDA events on seeded synthetic complex Gaussian matrices at the caller's
 // batch size, the fastest shape is stored in the handle, and the table can be
 // saved to / loaded from a text file keyed by device name and SM count.
@@ -97,14 +97,14 @@ extern "C" TOKURA_API int tokuraAutotune(tokurablas_t* handle, int n_min, int n_
   double2* eig = static_cast<double2*>(b.p[1]);
   double2* work = static_cast<double2*>(b.p[2]);
   char* flag = static_cast<char*>(b.p[3]);
-  static const int kLanes[4] = {1, 2, 4, 8};
+  static const int kLanes[6] = {1, 2, 4, 8, 16, 32};
   static const int kThreads[4] = {32, 64, 128, 256};
   for (int n = n_min; n <= n_max; ++n) {
     const long long count = (long long)n * n * batch_count;
     fill_cgauss_kernel<<<handle->sm_count * 4, 256, 0, stream>>>(A, count, 0x5eed0000ULL + n);
     float best = 1e30f;
     PlainConfig best_cfg{1, 64};
-    for (int li = 0; li < 4; ++li) {
+    for (int li = 0; li < 6; ++li) {
       if (n <= 2 && kLanes[li] > 1) continue;
       for (int ti = 0; ti < 4; ++ti) {
         PlainConfig cfg{kLanes[li], kThreads[ti]};
@@ -212,7 +212,7 @@ extern "C" TOKURA_API int tokuraLoadTuning(tokurablas_t* handle, const char* pat
     if (std::strcmp(word, "plain") == 0) {
       int n, lanes, threads;
       if (std::fscanf(f, "%d %d %d", &n, &lanes, &threads) != 3 || n < 1 || n > 64 ||
-          !(lanes == 1 || lanes == 2 || lanes == 4 || lanes == 8) || threads < 32 || threads > 256 || threads % 32) {
+          !plain_lanes_valid(lanes, false) || threads < 32 || threads > 256 || threads % 32) {
         status = 2;
         break;
       }

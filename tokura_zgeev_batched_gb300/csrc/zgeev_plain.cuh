@@ -91,7 +91,7 @@ __global__ void __launch_bounds__(256) zgeev_plain_kernel(int n, int batch, Batc
                                                            char* __restrict__ flag, int itmax, int balance,
                                                            const float2* __restrict__ est, int* __restrict__ state,
                                                            int scaled, int stage_tw) {
-  constexpr int TW = 32 / L;
+  constexpr int TW = 32 / L;  // matrices per warp (1 at 32 lanes)
   const int lane = threadIdx.x & 31;
   const long long warp = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const long long j = warp * TW + lane / L;
@@ -190,6 +190,16 @@ inline cudaError_t launch_plain_phase(int L, bool bal, unsigned blocks, int thre
                                                         carveout, scaled, stage_tw)
                : launch_plain_l<8, false, kPhase>(blocks, threads, stream, n, batch, B, work, flag, itmax, 0, est, state,
                                                            carveout, scaled, stage_tw);
+    case 16:
+      return b ? launch_plain_l<16, kB, kPhase>(blocks, threads, stream, n, batch, B, work, flag, itmax, bv, est, state,
+                                                        carveout, scaled, stage_tw)
+               : launch_plain_l<16, false, kPhase>(blocks, threads, stream, n, batch, B, work, flag, itmax, 0, est, state,
+                                                           carveout, scaled, stage_tw);
+    case 32:
+      return b ? launch_plain_l<32, kB, kPhase>(blocks, threads, stream, n, batch, B, work, flag, itmax, bv, est, state,
+                                                        carveout, scaled, stage_tw)
+               : launch_plain_l<32, false, kPhase>(blocks, threads, stream, n, batch, B, work, flag, itmax, 0, est, state,
+                                                           carveout, scaled, stage_tw);
     default:
       return cudaErrorInvalidValue;
   }
@@ -204,7 +214,7 @@ cudaError_t launch_batch(const PlainConfig& cfg, int n, int batch, const Batch& 
   const int L = cfg.lanes;
   // Lanes per matrix of the QR phase when it runs as its own launch (with hints).
   const int Lq = cfg.qr_lanes > 0 ? cfg.qr_lanes : L;
-  auto valid_lanes = [](int l) { return l == 1 || l == 2 || l == 4 || l == 8; };
+  auto valid_lanes = [](int l) { return l == 1 || l == 2 || l == 4 || l == 8 || l == 16 || l == 32; };
   if (!valid_lanes(L) || !valid_lanes(Lq)) return cudaErrorInvalidValue;
   const int tw = 32 / L;
   const int threads = cfg.threads;
