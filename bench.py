@@ -1009,6 +1009,27 @@ def run_ours(args):
         A_host.copy_(A)
         torch.cuda.synchronize()
 
+        def huge_page_share(t) -> float | None:
+            """Share of a host tensor's mapping backed by transparent huge pages (/proc/self/smaps);
+            without them the host link's rate after idle periods depends on the box."""
+            addr, inside, size, huge = t.data_ptr(), False, 0, 0
+            try:
+                with open("/proc/self/smaps") as f:
+                    for line in f:
+                        head = line.split(None, 1)[0]
+                        if "-" in head and not head.endswith(":"):
+                            lo, hi = (int(x, 16) for x in head.split("-"))
+                            inside = lo <= addr < hi
+                        elif inside and head == "Size:":
+                            size = int(line.split()[1])
+                        elif inside and head == "AnonHugePages:":
+                            huge = int(line.split()[1])
+            except (OSError, ValueError):
+                return None
+            return huge / size if size else None
+
+        host_huge = huge_page_share(A_host)
+
         def h2d_rate():
             """The host link's rate now (one pinned copy of the whole input), GB/s."""
             c0 = torch.cuda.Event(enable_timing=True)
@@ -1067,7 +1088,7 @@ def run_ours(args):
                "api": "tokura_zgeev_batched_host (pinned host buffers, wall clock)", "host_buffers": host_buffers,
                "flagged": host_flagged,
                "single_stream": {"value": ws * BATCH / (single_ms * 1e-3), "ms_per_step": single_ms},
-               "h2d_gbs": h2d_gbs}
+               "h2d_gbs": h2d_gbs, "host_input_huge_page_share": host_huge}
         del A_host, eig_host, flag_host
     del A, eig, flag, work
     torch.cuda.empty_cache()
