@@ -774,21 +774,34 @@ def measure_ragged(h, dev, stream, peak, batch: int = 200000) -> dict:
         plan[i].append(k)
         load[i] += float(counts[k]) * k ** 3
 
-    def per_size_concurrent():
+    def per_size_concurrent(hs):
         for i in range(CONC_STREAMS):
             streams[i].wait_stream(stream)
             for k in plan[i]:
                 p0, e0 = starts[k]
-                st = api.tokura_zgeev_batched_gpu(handles[i], k, int(counts[k]), A.data_ptr() + 16 * p0,
+                st = api.tokura_zgeev_batched_gpu(hs[i], k, int(counts[k]), A.data_ptr() + 16 * p0,
                                                   eig2.data_ptr() + 16 * e0, works[i].data_ptr(),
                                                   flag2.data_ptr() + int(fbase[k - 1]), streams[i].cuda_stream)
                 assert st == 0
         for i in range(CONC_STREAMS):
             stream.wait_stream(streams[i])
 
-    ms_conc = time_ms(per_size_concurrent, 2, stream)
+    ms_conc_default = time_ms(lambda: per_size_concurrent(handles), 2, stream)
     conc_same = bool(torch.equal(flag2, flag2_serial) and torch.equal(eig2, eig2_serial))
-    del works, handles
+    # The library's shapes assume a launch has the GPU to itself and widen small batches to up to
+    # 32 lanes per matrix; eight launches sharing the GPU do better with at most 4 lanes. The
+    # stronger of the two concurrent variants is the comparator.
+    want = torch.cuda.get_device_properties(dev).multi_processor_count * 4 * 2 * 32
+    capped = [api.Handle() for _ in range(CONC_STREAMS)]
+    for i in range(CONC_STREAMS):
+        for k in plan[i]:
+            c = int(counts[k])
+            lanes = 1 if (k <= 2 or c >= want) else (2 if 2 * c >= want else 4)
+            assert capped[i].set_plain_config(k, lanes, 32) == 0
+    ms_conc_capped = time_ms(lambda: per_size_concurrent(capped), 2, stream)
+    capped_flags_same = bool(torch.equal(flag2, flag2_serial))
+    ms_conc = min(ms_conc_default, ms_conc_capped)
+    del works, handles, capped
     work_flops = float(np.sum(40.0 * ns.astype(np.float64) ** 3))
     best = graph_ms if isinstance(graph_ms, float) else ms_ragged
     return {"batch": batch, "total_elements": total, "ms_ragged": ms_ragged, "ms_ragged_graph": graph_ms,
@@ -797,7 +810,9 @@ def measure_ragged(h, dev, stream, peak, batch: int = 200000) -> dict:
             "ms_per_size_plain_concurrent": ms_conc, "speedup_vs_per_size_concurrent": ms_conc / best,
             "per_size_concurrent": f"the 64 plain launches over {CONC_STREAMS} streams, one handle and one "
                                    f"workspace each, sizes dealt largest work first to the least-loaded stream; "
-                                   f"results bitwise equal to the serial launches: {conc_same}",
+                                   f"the faster of the library's launch shapes ({ms_conc_default:.1f} ms, results "
+                                   f"bitwise equal to the serial launches: {conc_same}) and at most 4 lanes per "
+                                   f"matrix ({ms_conc_capped:.1f} ms, flags equal: {capped_flags_same})",
             "fp64_frac": work_flops / (best * 1e-3) / peak, "flagged": flagged,
             "plain_launches": int(np.count_nonzero(counts)), "parity": parity,
             "shift_hints": "FP32 estimates for orders >= 48 (the default); the per-size plain launches use them "
