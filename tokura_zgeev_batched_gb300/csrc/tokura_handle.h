@@ -127,12 +127,14 @@ inline int group_lanes_for(const tokurablas_t* h, int n, int batch) {
 }
 
 // Launch shape of the real kernel: a tuned entry, else the lane heuristic of
-// the complex kernel (it depends on the batch size, not on the arithmetic).
+// the complex kernel (it depends on the batch size, not on the arithmetic),
+// up to the real kernel's 8 lanes per matrix.
 inline PlainConfig real_config_for(const tokurablas_t* h, int n, int batch) {
   PlainConfig c = h->real[n];
   if (c.lanes == 0) {
     const long long want_lanes = (long long)h->sm_count * 4 * 2 * 32;
     c.lanes = (long long)batch >= want_lanes ? 1 : ((long long)batch * 2 >= want_lanes ? 2 : 4);
+    if (c.lanes == 4 && (long long)batch * 4 < want_lanes && n >= 16) c.lanes = 8;
     if (n <= 2) c.lanes = 1;
   }
   if (c.threads == 0) c.threads = 32;
